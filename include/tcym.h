@@ -1,0 +1,173 @@
+/*
+ * tcym.h — C ABI of the GB300-native real-time lattice Yang-Mills hot path
+ * (SU(2)/SU(3) on a periodic 3D lattice): the drop-in for the GaugeLinks /
+ * ElectricFields objects and the Dynamics, LangevinDynamics, GradientFlow,
+ * GaussLawRestoration, Observables and Chern-Simons-rate calls of
+ * markmace/TopologicalCYMSolver.
+ *
+ * Plain C: opaque handles, pointers and sizes, int status codes.  Host arrays
+ * passed to upload/download use the reference's own AoS FP64 layouts:
+ *   U: V*3*NMD doubles, link (x,y,z,mu) at NMD*(mu + 3*site), NMD = 4 for SU(2)
+ *      (u0,u1,u2,u3 with U = u3 + i u_k sigma_k) or 18 for SU(3) (9 complex,
+ *      column-major (i,j) -> i + 3j)          (LATTICE/GaugeLinks.cpp:27-47)
+ *   E: V*3*NA doubles, E^a_mu(x) at a + NA*(mu + 3*site), NA = 3 or 8
+ *                                             (LATTICE/ElectricFields.cpp:36-46)
+ *   site = x + Nx*(y + Ny*z)
+ * The device copy is private to the library (structure-of-arrays; FP32 or FP64).
+ *
+ * Threading: a context owns a CUDA device; every lattice has its own stream.
+ * Calls on different lattices may run concurrently from different threads;
+ * calls on one lattice must be serialised by the caller.  No call exits or
+ * aborts: every failure is a status code with a message in tcym_last_error().
+ */
+#ifndef TCYM_H
+#define TCYM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TCYM_VERSION 100
+
+/* status codes */
+enum {
+    TCYM_OK = 0,
+    TCYM_ERR_ARG = 1,        /* invalid argument */
+    TCYM_ERR_OOM = 2,        /* device allocation failed */
+    TCYM_ERR_CUDA = 3,       /* CUDA runtime error (message has the CUDA string) */
+    TCYM_ERR_NONFINITE = 4,  /* a reduction saw NaN/Inf: the state is unhealthy */
+    TCYM_ERR_TIMEOUT = 5,    /* a bounded wait on device progress ran out */
+    TCYM_ERR_ADMISSION = 6,  /* the serving loop refused a request (HBM budget) */
+    TCYM_ERR_STATE = 7       /* call not valid in the object's state */
+};
+
+/* storage precision of a lattice */
+enum {
+    TCYM_FP64 = 0, /* FP64 links and fields: the plain drop-in */
+    TCYM_FP32 = 1  /* FP32 storage (SU(3): two rows), FP64 reductions and reunitarisation */
+};
+
+/* gradient-flow sweep order */
+enum {
+    TCYM_FLOW_SIMULTANEOUS = 0, /* all links at once, as GradientFlow::StandardUpdate */
+    TCYM_FLOW_CHECKERBOARD = 1  /* six in-place sub-sweeps by (site parity, direction) */
+};
+
+typedef struct tcym_ctx_s *tcym_ctx;
+typedef struct tcym_lattice_s *tcym_lattice;
+
+/* FP64 observables of one lattice (all spacings 1 -> metric factors 1):
+ * Observables::Bulk (OBSERVABLES/BulkObservables.cpp:29-143),
+ * Observables::GaussLaw (GaussLawViolation.cpp:13-61),
+ * Observables::Unitarity (UnitarityViolation.cpp:13-51),
+ * UnimprovedOperators::ComputeEDotB (CALC/ChernSimonsOperators.cpp:4-47). */
+typedef struct {
+    double T00;          /* energy density: Bulk::T00() */
+    double electric;     /* Bulk::ELECTRIC() */
+    double magnetic;     /* Bulk::MAGNETIC() */
+    double esqr[3];      /* Bulk::ESqr[mu]: <sum_a E^a_mu E^a_mu> */
+    double bsqr[3];      /* Bulk::BSqr[i]:  <4 Re tr(1 - P_jk)> */
+    double gauss_max;    /* GaussLaw::GlobalMaxViolation (signed maximum, from 0) */
+    double gauss_rms;    /* GaussLaw::GlobalAvgViolation */
+    double gauss_absmax; /* max |G^a(x)| (no reference counterpart) */
+    double unit_max;     /* Unitarity::GlobalMaxViolation */
+    double unit_rms;     /* Unitarity::GlobalAvgViolation */
+    double edotb;        /* sum_x E.B with the clover operator */
+    double ncs_dot;      /* edotb / (8 pi^2): ChernSimonsNumber::NCsDot (TOPOLOGY/ChernSimonsDerivative.cpp:31-49) */
+    double ncs;          /* Kahan-compensated integral of ncs_dot dt tracked during steps */
+    int nonfinite;       /* 1 when any reduced quantity was NaN/Inf */
+} tcym_obs;
+
+int tcym_version(void);
+
+/* ---------------------------------------------------------------- context */
+/* Opens a context on CUDA device `device`. */
+int tcym_ctx_create(int device, tcym_ctx *out);
+int tcym_ctx_destroy(tcym_ctx ctx);
+/* Message of the last failure on this context (valid until the next call). */
+const char *tcym_last_error(tcym_ctx ctx);
+
+/* ---------------------------------------------------------------- lattices */
+/* GaugeLinks(Nx,Ny,Nz,ax,ay,az) + ElectricFields(...) (LATTICE/GaugeLinks.cpp:65-81,
+ * LATTICE/ElectricFields.cpp:66-82): allocates links (ping-pong pair) and fields on the
+ * device.  nc = 2 or 3; spacings a = 1. Contents are undefined until set. */
+int tcym_lattice_create(tcym_ctx ctx, int nc, int nx, int ny, int nz, int precision, tcym_lattice *out);
+/* as tcym_lattice_create with lattice spacings a[3] (reference: integer spacings). */
+int tcym_lattice_create_ex(tcym_ctx ctx, int nc, int nx, int ny, int nz, const double a[3], int precision,
+                           tcym_lattice *out);
+int tcym_lattice_destroy(tcym_lattice lat);
+/* device bytes held by the lattice (links, fields, scratch) */
+int tcym_lattice_bytes(tcym_lattice lat, size_t *bytes);
+/* Copies host AoS FP64 arrays in (either may be NULL), converting to the storage format. */
+int tcym_lattice_upload(tcym_lattice lat, const double *U_aos, const double *E_aos);
+/* Copies the state out to host AoS FP64 arrays (either may be NULL). */
+int tcym_lattice_download(tcym_lattice lat, double *U_aos, double *E_aos);
+/* dst <- src (same group and extents; any precisions): Copy() of GaugeLinks.cpp:91-107
+ * and ElectricFields.cpp:90-104. */
+int tcym_lattice_copy(tcym_lattice dst, const tcym_lattice src);
+/* Waits for all work queued on the lattice. */
+int tcym_lattice_sync(tcym_lattice lat);
+
+/* ------------------------------------------------------ initial conditions */
+/* InitialConditions::SetZero (INITIALCONDITIONS/SetZero.cpp:3-24): U = 1, E = 0. */
+int tcym_set_zero(tcym_lattice lat);
+/* E^a_mu(x) = sigma * N(0,1) from the Philox field stream of `seed`; with
+ * sigma = 1/sqrt(beta) this is ThermalDynamics::ReassignElectricFields before its
+ * Gauss restore (DYNAMICS/ThermalDynamics.cpp:205-226). */
+int tcym_gaussian_efield(tcym_lattice lat, double sigma, uint64_t seed);
+/* U_mu(x) = exp(i t^a theta^a), theta^a = sigma * N(0,1) from the Philox link stream. */
+int tcym_random_links(tcym_lattice lat, double sigma, uint64_t seed);
+/* GaussLawRestoration::Restore (GAUSSLAWFIXING/GaussRestore.cpp:131-167): iterate
+ * E -= g (G(x) - Adj(U) G(x+mu)), g = 7/24, 7/48, 7/72, until the signed maximum
+ * of G is <= tol (reference: 1e-14) or maxit iterations (reference: 10000).
+ * iters / final_max may be NULL. */
+int tcym_gauss_restore(tcym_lattice lat, double tol, int maxit, int *iters, double *final_max);
+
+/* --------------------------------------------------------------- dynamics */
+/* Dynamics::Update(U,E) (DYNAMICS/Dynamics.cpp:204-218), nsteps times: E update from
+ * the plaquettes (Dynamics.cpp:145-197) then U <- exp(-i dt E) U (Dynamics.cpp:97-138),
+ * fused in one kernel per step. */
+int tcym_leapfrog(tcym_lattice lat, double dt, int nsteps);
+/* Dynamics::UpdateElectricFields over the whole lattice (Dynamics.cpp:145-197). */
+int tcym_update_e(tcym_lattice lat, double dt);
+/* Dynamics::UpdateGaugeLinks over the whole lattice (Dynamics.cpp:97-138). */
+int tcym_update_u(tcym_lattice lat, double dt);
+/* LangevinDynamics::Update() without its periodic prints (DYNAMICS/LangevinDynamics.cpp:
+ * 260-347): E += dt F - gamma dt E + sqrt(gamma dt) sqrt(2T) xi, then the link update,
+ * for steps step0 .. step0+nsteps-1.  xi ~ N(0,1) drawn in-kernel from the Philox noise
+ * stream keyed by (seed, step, site, mu, colour).  The reference has gamma = 1 and
+ * beta = 1/T (LangevinDynamics.cpp:23,184-186). */
+int tcym_langevin(tcym_lattice lat, double dt, double gamma, double T, uint64_t seed, uint64_t step0, int nsteps);
+/* GradientFlow::StandardUpdate (calibrate = 0) / CalibrationUpdate (calibrate = 1)
+ * (GRADIENTFLOW/GradientFlow.cpp:150-188), nsteps flow steps of size dtau (the
+ * reference's DcTau = SqrtDcTauOverSpacing^2), all links at once or checkerboarded.
+ * With calibrate, *dncs receives sum dtau/2 [NCsDot(U,F) + NCsDot(U',F)] using the
+ * clover operator.  The field array holds the last flow force afterwards, as in the
+ * reference.  Checkerboard mode needs even extents. */
+int tcym_flow(tcym_lattice lat, double dtau, int nsteps, int mode, int calibrate, double *dncs);
+/* Projects every stored link back onto the group in FP64 (no reference counterpart). */
+int tcym_reunitarize(tcym_lattice lat);
+/* Reunitarise automatically every `period` steps of leapfrog/Langevin (0 = never).
+ * Default: 100 for TCYM_FP32 lattices, 0 for TCYM_FP64. */
+int tcym_set_reunitarize_period(tcym_lattice lat, int period);
+
+/* ------------------------------------------------------------ observables */
+/* All observables of the current state (FP64 reductions, fixed order). Returns
+ * TCYM_ERR_NONFINITE (with *out filled) when a reduced value is NaN/Inf. */
+int tcym_observables(tcym_lattice lat, tcym_obs *out);
+/* UnimprovedOperators::ComputeEDotB (CALC/ChernSimonsOperators.cpp:4-47): sum_x E.B, clover. */
+int tcym_edotb(tcym_lattice lat, double *out);
+/* Track N_CS during leapfrog/Langevin steps: every `every` steps (0 = off) add
+ * every*dt * NCsDot of the new state to a Kahan-compensated FP64 sum on the device. */
+int tcym_ncs_track(tcym_lattice lat, int every);
+int tcym_ncs_get(tcym_lattice lat, double *ncs);
+int tcym_ncs_reset(tcym_lattice lat);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TCYM_H */

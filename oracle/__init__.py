@@ -1,0 +1,258 @@
+"""ORACLE — test infrastructure, not product.
+
+ctypes bindings for
+  * ``liboracle.so``: the FP64 C restatement of the reference's hot path
+    (tcym_oracle.c), built by ``make -C oracle`` on any host;
+  * ``_ref/libref_su{2,3}.so``: the reference's own sources compiled in place
+    (ref_wrap.cpp), present only where the reference tree was available.
+
+Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU legs import this.
+Arrays are the reference's AoS FP64 layouts:
+  U: (V, 3, NM) doubles, NM = 4 (SU(2) quaternion) or 18 (SU(3), 9 complex, column-major)
+  E: (V, 3, NA) doubles, NA = 3 or 8
+with site index x + Nx*(y + Ny*z).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+_dbl_p = ctypes.POINTER(ctypes.c_double)
+_int_p = ctypes.POINTER(ctypes.c_int)
+
+NM = {2: 4, 3: 18}
+NA = {2: 3, 3: 8}
+OBS_FIELDS = ("T00", "ELECTRIC", "MAGNETIC", "E0", "E1", "E2", "B0", "B1", "B2",
+              "gauss_max", "gauss_rms", "unit_max", "unit_rms", "edotb_clover",
+              "edotb_improved", "gauss_absmax")
+
+
+def build(quiet: bool = True) -> None:
+    """Compile liboracle.so (and the reference libs when the reference tree exists)."""
+    out = subprocess.DEVNULL if quiet else None
+    subprocess.run(["make", "-s", "-C", HERE], check=True, stdout=out)
+    ref_tree = os.environ.get("REFERENCE", "/root/reference")
+    if os.path.isdir(ref_tree):
+        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REFERENCE={ref_tree}"], check=True, stdout=out)
+
+
+def _p(a: np.ndarray):
+    assert a.dtype == np.float64 and a.flags.c_contiguous
+    return a.ctypes.data_as(_dbl_p)
+
+
+def _n(shape):
+    return (ctypes.c_int * 3)(*shape)
+
+
+def empty_fields(nc: int, shape):
+    V = int(np.prod(shape))
+    return np.zeros((V, 3, NM[nc])), np.zeros((V, 3, NA[nc]))
+
+
+class Port:
+    """The C restatement for one gauge group (2 or 3)."""
+
+    def __init__(self, nc: int):
+        path = os.path.join(HERE, "liboracle.so")
+        if not os.path.exists(path):
+            build()
+        self.lib = ctypes.CDLL(path)
+        self.nc = nc
+        self.g = f"orc_su{nc}_"
+        L = self.lib
+        f = self._f
+        f("leapfrog").argtypes = [_int_p, _dbl_p, _dbl_p, ctypes.c_double, ctypes.c_int]
+        f("update_e_only").argtypes = [_int_p, _dbl_p, _dbl_p, ctypes.c_double]
+        f("update_u_only").argtypes = [_int_p, _dbl_p, _dbl_p, ctypes.c_double]
+        f("langevin").argtypes = [_int_p, _dbl_p, _dbl_p, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                  ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int]
+        f("flow").argtypes = [_int_p, _dbl_p, _dbl_p, ctypes.c_double, ctypes.c_int, ctypes.c_int]
+        f("flow").restype = ctypes.c_double
+        f("flow_checkerboard").argtypes = [_int_p, _dbl_p, ctypes.c_double, ctypes.c_int]
+        f("gauss_restore").argtypes = [_int_p, _dbl_p, _dbl_p, ctypes.c_double, ctypes.c_int]
+        f("gauss_restore").restype = ctypes.c_int
+        f("observables").argtypes = [_int_p, _dbl_p, _dbl_p, _dbl_p]
+        f("edotb_clover").argtypes = [_int_p, _dbl_p, _dbl_p]
+        f("edotb_clover").restype = ctypes.c_double
+        f("set_zero").argtypes = [_int_p, _dbl_p, _dbl_p]
+        f("gaussian_efield").argtypes = [_int_p, _dbl_p, ctypes.c_double, ctypes.c_uint64]
+        f("random_links").argtypes = [_int_p, _dbl_p, ctypes.c_double, ctypes.c_uint64]
+        f("matrix_iexp").argtypes = [ctypes.c_double, _dbl_p, _dbl_p]
+        f("retr_igen").argtypes = [_dbl_p, _dbl_p]
+        f("adjoint").argtypes = [_dbl_p, _dbl_p, _dbl_p]
+        f("inverse_adjoint").argtypes = [_dbl_p, _dbl_p, _dbl_p]
+        L.orc_normal_c.argtypes = [ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_uint32,
+                                   ctypes.c_uint32, ctypes.c_uint32]
+        L.orc_normal_c.restype = ctypes.c_double
+        L.orc_philox4x32.argtypes = [ctypes.POINTER(ctypes.c_uint32)] * 3
+
+    def _f(self, name):
+        return getattr(self.lib, self.g + name)
+
+    # lattice-level calls (arrays modified in place)
+    def leapfrog(self, shape, U, E, dt, nsteps):
+        self._f("leapfrog")(_n(shape), _p(U), _p(E), dt, nsteps)
+
+    def update_e(self, shape, U, E, dt):
+        self._f("update_e_only")(_n(shape), _p(U), _p(E), dt)
+
+    def update_u(self, shape, U, E, dt):
+        self._f("update_u_only")(_n(shape), _p(U), _p(E), dt)
+
+    def langevin(self, shape, U, E, dt, gamma, T, seed, step0, nsteps):
+        self._f("langevin")(_n(shape), _p(U), _p(E), dt, gamma, T, seed, step0, nsteps)
+
+    def flow(self, shape, U, E, dtau, nsteps, calibrate=0):
+        return self._f("flow")(_n(shape), _p(U), _p(E), dtau, nsteps, calibrate)
+
+    def flow_checkerboard(self, shape, U, dtau, nsweeps):
+        self._f("flow_checkerboard")(_n(shape), _p(U), dtau, nsweeps)
+
+    def gauss_restore(self, shape, U, E, tol=1e-14, maxit=10000):
+        return self._f("gauss_restore")(_n(shape), _p(U), _p(E), tol, maxit)
+
+    def observables(self, shape, U, E):
+        out = np.zeros(16)
+        self._f("observables")(_n(shape), _p(U), _p(E), _p(out))
+        return out
+
+    def edotb_clover(self, shape, U, E):
+        return self._f("edotb_clover")(_n(shape), _p(U), _p(E))
+
+    def set_zero(self, shape, U, E):
+        self._f("set_zero")(_n(shape), _p(U), _p(E))
+
+    def gaussian_efield(self, shape, E, sigma, seed):
+        self._f("gaussian_efield")(_n(shape), _p(E), sigma, seed)
+
+    def random_links(self, shape, U, sigma, seed):
+        self._f("random_links")(_n(shape), _p(U), sigma, seed)
+
+    # single objects
+    def matrix_iexp(self, c, alpha):
+        out = np.zeros(NM[self.nc])
+        self._f("matrix_iexp")(c, _p(np.ascontiguousarray(alpha, dtype=np.float64)), _p(out))
+        return out
+
+    def retr_igen(self, v):
+        out = np.zeros(NA[self.nc])
+        self._f("retr_igen")(_p(np.ascontiguousarray(v, dtype=np.float64)), _p(out))
+        return out
+
+    def adjoint(self, v, e):
+        out = np.zeros(NA[self.nc])
+        self._f("adjoint")(_p(np.ascontiguousarray(v, dtype=np.float64)), _p(np.ascontiguousarray(e, dtype=np.float64)), _p(out))
+        return out
+
+    def inverse_adjoint(self, v, e):
+        out = np.zeros(NA[self.nc])
+        self._f("inverse_adjoint")(_p(np.ascontiguousarray(v, dtype=np.float64)), _p(np.ascontiguousarray(e, dtype=np.float64)), _p(out))
+        return out
+
+    def normal(self, seed, stream, step, site, mu, a):
+        return self.lib.orc_normal_c(seed, stream, step, site, mu, a)
+
+    def philox(self, ctr, key):
+        c = (ctypes.c_uint32 * 4)(*ctr)
+        k = (ctypes.c_uint32 * 2)(*key)
+        o = (ctypes.c_uint32 * 4)()
+        self.lib.orc_philox4x32(c, k, o)
+        return list(o)
+
+
+def ref_available(nc: int) -> bool:
+    return os.path.exists(os.path.join(HERE, "_ref", f"libref_su{nc}.so"))
+
+
+class Ref:
+    """The reference's own sources, compiled in place (only where the reference tree exists).
+
+    The reference keeps its lattice in globals, so one instance per group and one
+    lattice at a time."""
+
+    def __init__(self, nc: int):
+        path = os.path.join(HERE, "_ref", f"libref_su{nc}.so")
+        self.lib = L = ctypes.CDLL(path)
+        self.nc = nc
+        L.ref_init.argtypes = [ctypes.c_int] * 3
+        L.ref_set.argtypes = [_dbl_p, _dbl_p]
+        L.ref_get.argtypes = [_dbl_p, _dbl_p]
+        L.ref_leapfrog.argtypes = [ctypes.c_double, ctypes.c_int]
+        L.ref_update_e.argtypes = [ctypes.c_double]
+        L.ref_update_u.argtypes = [ctypes.c_double]
+        L.ref_langevin.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int]
+        L.ref_flow.argtypes = [ctypes.c_double, ctypes.c_int, ctypes.c_int]
+        L.ref_flow.restype = ctypes.c_double
+        L.ref_thermal_efield.argtypes = [ctypes.c_double, ctypes.c_uint64]
+        L.ref_observables.argtypes = [_dbl_p]
+        L.ref_matrix_iexp.argtypes = [ctypes.c_double, _dbl_p, _dbl_p]
+        L.ref_retr_igen.argtypes = [_dbl_p, _dbl_p]
+        L.ref_adjoint.argtypes = [_dbl_p, _dbl_p, _dbl_p]
+        L.ref_inverse_adjoint.argtypes = [_dbl_p, _dbl_p, _dbl_p]
+        self.shape = None
+
+    def init(self, shape):
+        self.shape = tuple(shape)
+        self.lib.ref_init(*shape)
+
+    def set(self, U, E):
+        self.lib.ref_set(_p(U), _p(E))
+
+    def get(self):
+        U, E = empty_fields(self.nc, self.shape)
+        self.lib.ref_get(_p(U), _p(E))
+        return U, E
+
+    def set_zero(self):
+        self.lib.ref_set_zero()
+
+    def leapfrog(self, dt, nsteps):
+        self.lib.ref_leapfrog(dt, nsteps)
+
+    def update_e(self, dt):
+        self.lib.ref_update_e(dt)
+
+    def update_u(self, dt):
+        self.lib.ref_update_u(dt)
+
+    def langevin(self, dt, T, seed, step0, nsteps):
+        self.lib.ref_langevin(dt, T, seed, step0, nsteps)
+
+    def flow(self, sqrt_dtau, nsteps, calibrate=0):
+        return self.lib.ref_flow(sqrt_dtau, nsteps, calibrate)
+
+    def gauss_restore(self):
+        self.lib.ref_gauss_restore()
+
+    def thermal_efield(self, beta, seed):
+        self.lib.ref_thermal_efield(beta, seed)
+
+    def observables(self):
+        out = np.zeros(16)
+        self.lib.ref_observables(_p(out))
+        return out
+
+    def matrix_iexp(self, c, alpha):
+        out = np.zeros(NM[self.nc])
+        self.lib.ref_matrix_iexp(c, _p(np.ascontiguousarray(alpha, dtype=np.float64)), _p(out))
+        return out
+
+    def retr_igen(self, v):
+        out = np.zeros(NA[self.nc])
+        self.lib.ref_retr_igen(_p(np.ascontiguousarray(v, dtype=np.float64)), _p(out))
+        return out
+
+    def adjoint(self, v, e):
+        out = np.zeros(NA[self.nc])
+        self.lib.ref_adjoint(_p(np.ascontiguousarray(v, dtype=np.float64)), _p(np.ascontiguousarray(e, dtype=np.float64)), _p(out))
+        return out
+
+    def inverse_adjoint(self, v, e):
+        out = np.zeros(NA[self.nc])
+        self.lib.ref_inverse_adjoint(_p(np.ascontiguousarray(v, dtype=np.float64)), _p(np.ascontiguousarray(e, dtype=np.float64)), _p(out))
+        return out

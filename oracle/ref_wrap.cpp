@@ -1,0 +1,224 @@
+/*
+ * ORACLE (test infrastructure only; never part of the product).
+ *
+ * Compiles the reference's own real-time hot-path sources, in place, into a
+ * C-callable shared library oracle/_ref/libref_su{2,3}.so.  The reference is a
+ * unity build (every module is a .cpp #included into one translation unit,
+ * SphaleronSimulation.cpp:13-202); this file is such a translation unit that
+ * pulls in only the hot-path modules, in the reference's include order, from
+ * the reference tree given by -I (see oracle/Makefile).  Nothing of the
+ * reference is copied.
+ *
+ * Substitutions, each outside the reference's arithmetic:
+ *   - <mpi.h>, "fftw3.h": empty shims (oracle/shim), the hot path calls neither.
+ *   - GSL: namespace RandomNumberGenerator is supplied here, drawing Philox
+ *     normals (orc_philox.h) so that the noise is the same stream the CUDA
+ *     kernels draw (MISC/RNG/GSLRandomNumberGenerator.cpp is not included).
+ *   - LAPACK zgeev: a stub that aborts; it is reached only from MatrixILog
+ *     (SUNc/SU3/AlgebraOperations.cpp:186-233), which is off this path.
+ *   - The time steps Dynamics::dTau (DYNAMICS/Dynamics.cpp:17),
+ *     LangevinDynamics::dTauL (DYNAMICS/LangevinDynamics.cpp:41) and
+ *     ThermalDynamics::dTau (DYNAMICS/ThermalDynamics.cpp:23) are declared
+ *     `static const`; `const` is defined away around those three includes so
+ *     the step can be set at run time.  Each file has no other `const`.
+ */
+#include "Definitions.cpp"
+
+#ifndef SU_Nc_FLAG
+#error "build with -DSU_Nc_FLAG=SU2_FLAG or -DSU_Nc_FLAG=SU3_FLAG"
+#endif
+#define METRIC_FLAG MINKOWSKI_FLAG
+
+#include <cstdint>
+#include <cstdio>
+
+#include "SUNc/Definitions.cpp"
+#include "orc_philox.h"
+
+namespace RandomNumberGenerator {
+    long int MySEED = 0;
+    static uint64_t shim_seed = 0;
+    static uint32_t shim_stream = 0;
+    static uint64_t shim_step = 0;
+    static uint64_t shim_index = 0;
+
+    void Init(long int SEED) { MySEED = SEED; shim_seed = (uint64_t)SEED; shim_index = 0; }
+    void SetStream(uint64_t seed, uint32_t stream, uint64_t step) {
+        shim_seed = seed; shim_stream = stream; shim_step = step; shim_index = 0;
+    }
+    /* The i-th call returns the normal of E component i = a + NA*(mu + 3*site). */
+    DOUBLE Gauss() {
+        const uint64_t na = SUNcAlgebra::VectorSize;
+        uint64_t i = shim_index++;
+        uint32_t a = (uint32_t)(i % na);
+        uint32_t mu = (uint32_t)((i / na) % 3);
+        uint32_t site = (uint32_t)(i / (3 * na));
+        return orc_normal(shim_seed, shim_stream, shim_step, site, mu, a);
+    }
+    DOUBLE Gauss(DOUBLE Amplitude) { return Amplitude * Gauss(); }
+    DOUBLE rng() { std::fprintf(stderr, "oracle: uniform RNG is off the hot path\n"); std::abort(); }
+}
+
+#if SU_Nc_FLAG == SU3_FLAG
+extern "C" void zgeev(char const *, char const *, int *, COMPLEX *, int *, COMPLEX *, COMPLEX *, int *,
+                      COMPLEX *, int *, COMPLEX *, int *, double *, int *) {
+    std::fprintf(stderr, "oracle: zgeev (SU(3) matrix log) is off the hot path\n");
+    std::abort();
+}
+#endif
+
+#include "IO/StringManipulation.cpp"
+#include "IO/OutputManagement.cpp"
+#include "LATTICE/3DGrid.cpp"
+#include "LATTICE/GaugeLinks.cpp"
+#include "LATTICE/ElectricFields.cpp"
+#include "LATTICE/GLinksEFields.cpp"
+#include "LATTICE/Indexing.cpp"
+#include "CALC/Plaquettes.cpp"
+#include "CALC/AvgFieldStrength.cpp"
+#include "CALC/GaussViolation.cpp"
+#include "CALC/ChernSimonsOperators.cpp"
+#include "TOPOLOGY/ChernSimonsDerivative.cpp"
+DOUBLE Qs = 1.0;
+#define const
+#include "DYNAMICS/Dynamics.cpp"
+#undef const
+#include "OBSERVABLES/BulkObservables.cpp"
+#include "OBSERVABLES/GaussLawViolation.cpp"
+#include "OBSERVABLES/UnitarityViolation.cpp"
+#include "GAUSSLAWFIXING/GaussRestore.cpp"
+#include "INITIALCONDITIONS/SetZero.cpp"
+#define const
+#include "DYNAMICS/ThermalDynamics.cpp"
+#include "DYNAMICS/LangevinDynamics.cpp"
+#undef const
+#include "GRADIENTFLOW/GradientFlow.cpp"
+
+static bool g_langevin_ready = false;
+
+extern "C" {
+
+int ref_nc() { return Nc; }
+int ref_matrix_doubles() { return (int)(SUNcGroup::MatrixSize * sizeof(SU_Nc_FUNDAMENTAL_FORMAT) / sizeof(double)); }
+int ref_algebra_size() { return SUNcAlgebra::VectorSize; }
+
+/* Lattice::N/Volume must be set before Lattice::Init (SU2Solver.cpp:106-120). */
+void ref_init(int nx, int ny, int nz) {
+    if (GLinks::U) { delete GLinks::U; delete EFields::E; }
+    Lattice::N[0] = nx; Lattice::N[1] = ny; Lattice::N[2] = nz;
+    Lattice::Volume = nx * ny * nz;
+    Lattice::Init();
+    Dynamics::Reset();
+    LangevinDynamics::Reset();
+    GradientFlow::Reset();
+    if (g_langevin_ready) { delete LangevinVariables::Xi; g_langevin_ready = false; }
+}
+
+void ref_set(const double *U, const double *E) {
+    std::memcpy(GLinks::U->U, U, sizeof(SU_Nc_FUNDAMENTAL_FORMAT) * 3 * SUNcGroup::MatrixSize * GLinks::U->Volume);
+    std::memcpy(EFields::E->E, E, sizeof(double) * 3 * SUNcAlgebra::VectorSize * EFields::E->Volume);
+}
+
+void ref_get(double *U, double *E) {
+    std::memcpy(U, GLinks::U->U, sizeof(SU_Nc_FUNDAMENTAL_FORMAT) * 3 * SUNcGroup::MatrixSize * GLinks::U->Volume);
+    std::memcpy(E, EFields::E->E, sizeof(double) * 3 * SUNcAlgebra::VectorSize * EFields::E->Volume);
+}
+
+void ref_set_zero() { InitialConditions::SetZero(0, Lattice::N[0] - 1, 0, Lattice::N[1] - 1, 0, Lattice::N[2] - 1); }
+
+/* Dynamics::Update (DYNAMICS/Dynamics.cpp:204-218), nsteps times at time step dt. */
+void ref_leapfrog(double dt, int nsteps) {
+    Dynamics::dTau = dt;
+    for (int s = 0; s < nsteps; ++s) Dynamics::Update(GLinks::U, EFields::E);
+}
+
+/* E half-kick only (Dynamics.cpp:145-197), for unit parity of the force. */
+void ref_update_e(double dt) {
+    Dynamics::dTau = dt;
+    Dynamics::SetMetric();
+    Dynamics::UpdateElectricFields(0, Lattice::N[0] - 1, 0, Lattice::N[1] - 1, 0, Lattice::N[2] - 1, GLinks::U, EFields::E);
+}
+
+/* Link update only (Dynamics.cpp:97-138). */
+void ref_update_u(double dt) {
+    Dynamics::dTau = dt;
+    Dynamics::SetMetric();
+    Dynamics::UpdateGaugeLinks(0, Lattice::N[0] - 1, 0, Lattice::N[1] - 1, 0, Lattice::N[2] - 1, GLinks::U, EFields::E);
+}
+
+/* LangevinDynamics::UpdateRandomGaussianNoise + UpdateFields
+ * (DYNAMICS/LangevinDynamics.cpp:260-311); beta = 1/T (LangevinDynamics.cpp:23). */
+void ref_langevin(double dt, double T, uint64_t seed, uint64_t step0, int nsteps) {
+    if (!g_langevin_ready) { LangevinVariables::Init(); g_langevin_ready = true; }
+    LangevinDynamics::dTauL = dt;
+    LangevinDynamics::beta = 1.0 / T;
+    for (int s = 0; s < nsteps; ++s) {
+        RandomNumberGenerator::SetStream(seed, ORC_STREAM_NOISE, step0 + (uint64_t)s);
+        LangevinDynamics::UpdateRandomGaussianNoise();
+        LangevinDynamics::UpdateFields(GLinks::U, EFields::E);
+    }
+}
+
+/* GradientFlow::StandardUpdate / CalibrationUpdate (GRADIENTFLOW/GradientFlow.cpp:150-188).
+ * Returns ChernSimonsNumber::DeltaNCsCooling accumulated over the calibrated steps. */
+double ref_flow(double sqrt_dctau_over_a, int nsteps, int calibrate) {
+    GradientFlow::SqrtDcTauOverSpacing = sqrt_dctau_over_a;
+    GradientFlow::Reset();
+    ChernSimonsNumber::DeltaNCsCooling = 0.0;
+    for (int s = 0; s < nsteps; ++s) {
+        if (calibrate) GradientFlow::CalibrationUpdate(GLinks::U, EFields::E);
+        else GradientFlow::StandardUpdate(GLinks::U, EFields::E);
+    }
+    return ChernSimonsNumber::DeltaNCsCooling;
+}
+
+/* GaussLawRestoration::Restore (GAUSSLAWFIXING/GaussRestore.cpp:131-167). */
+void ref_gauss_restore() { GaussLawRestoration::Restore(GLinks::U, EFields::E); }
+
+/* ThermalDynamics::ReassignElectricFields (DYNAMICS/ThermalDynamics.cpp:205-226):
+ * E = N(0,1)/sqrt(beta) from the Philox field stream, then Gauss restore. */
+void ref_thermal_efield(double beta, uint64_t seed) {
+    ThermalDynamics::beta = beta;
+    RandomNumberGenerator::SetStream(seed, ORC_STREAM_EFIELD, 0);
+    ThermalDynamics::ReassignElectricFields();
+}
+
+/* Observables: Bulk (OBSERVABLES/BulkObservables.cpp:133-143), GaussLaw
+ * (GaussLawViolation.cpp:13-61), Unitarity (UnitarityViolation.cpp:13-51), and
+ * both E.B operators (CALC/ChernSimonsOperators.cpp:4-47, 72-382).
+ * out[0..14] = T00, ELECTRIC, MAGNETIC, ESqr[3], BSqr[3], gauss signed max,
+ * gauss rms, unitarity max, unitarity rms, clover E.B, improved E.B. */
+void ref_observables(double *out) {
+    Dynamics::SetMetric();
+    GaugeLinks *U = GLinks::U;
+    ElectricFields *E = EFields::E;
+    Observables::Bulk::Update(U, E);
+    out[0] = Observables::Bulk::T00();
+    out[1] = Observables::Bulk::ELECTRIC();
+    out[2] = Observables::Bulk::MAGNETIC();
+    for (int i = 0; i < 3; ++i) { out[3 + i] = Observables::Bulk::ESqr[i]; out[6 + i] = Observables::Bulk::BSqr[i]; }
+    Observables::GaussLaw::UpdateViolation(0, U->N[0] - 1, 0, U->N[1] - 1, 0, U->N[2] - 1, U, E);
+    out[9] = Observables::GaussLaw::GlobalMaxViolation;
+    out[10] = Observables::GaussLaw::GlobalAvgViolation;
+    Observables::Unitarity::UpdateViolation(0, U->N[0] - 1, 0, U->N[1] - 1, 0, U->N[2] - 1, U);
+    out[11] = Observables::Unitarity::GlobalMaxViolation;
+    out[12] = Observables::Unitarity::GlobalAvgViolation;
+    out[13] = UnimprovedOperators::ComputeEDotB(U, E);
+    out[14] = ImprovedOperators::ComputeEDotB(U, E);
+}
+
+/* Group kernels for unit tests of the device math. */
+void ref_matrix_iexp(double c, const double *alpha, double *out) {
+    SUNcAlgebra::Operations::MatrixIExp(c, (DOUBLE *)alpha, (SU_Nc_FUNDAMENTAL_FORMAT *)out);
+}
+void ref_retr_igen(const double *V, double *out) {
+    SUNcGroup::Operations::ReTrIGenU((SU_Nc_FUNDAMENTAL_FORMAT *)V, out);
+}
+void ref_inverse_adjoint(const double *V, const double *A, double *out) {
+    SUNcAlgebra::Operations::InverseAdjointMultiplication((SU_Nc_FUNDAMENTAL_FORMAT *)V, (DOUBLE *)A, out);
+}
+void ref_adjoint(const double *V, const double *A, double *out) {
+    SUNcAlgebra::Operations::AdjointMultiplication((SU_Nc_FUNDAMENTAL_FORMAT *)V, (DOUBLE *)A, out);
+}
+
+}  // extern "C"

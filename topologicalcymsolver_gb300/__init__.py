@@ -1,0 +1,280 @@
+"""GB300-native real-time lattice Yang-Mills hot path (SU(2)/SU(3)).
+
+Python mirror of the C ABI in ``include/tcym.h`` (libtcym.so, hand-written
+sm_103a CUDA kernels).  Names follow the reference's C++ interface
+(markmace/TopologicalCYMSolver): a :class:`Lattice` is the pair
+GaugeLinks + ElectricFields; its methods are Dynamics::Update,
+LangevinDynamics::Update, GradientFlow::StandardUpdate/CalibrationUpdate,
+GaussLawRestoration::Restore, Observables::* and the Chern-Simons rate.
+
+There is no CPU fallback: importing works anywhere, but creating a
+:class:`Context` loads libtcym.so and needs a CUDA device; every failure is
+raised as :class:`TcymError` with the library's message.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import build as _build
+
+__all__ = ["Context", "Lattice", "Observables", "TcymError", "FP32", "FP64", "FLOW_SIMULTANEOUS",
+           "FLOW_CHECKERBOARD", "library", "NM", "NA"]
+
+FP64, FP32 = 0, 1
+FLOW_SIMULTANEOUS, FLOW_CHECKERBOARD = 0, 1
+NM = {2: 4, 3: 18}   # doubles per link in the reference AoS layout
+NA = {2: 3, 3: 8}    # algebra components
+
+_ERRORS = {1: "invalid argument", 2: "device out of memory", 3: "CUDA error", 4: "non-finite state",
+           5: "timeout", 6: "admission refused", 7: "invalid state"}
+
+
+class TcymError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"tcym error {code} ({_ERRORS.get(code, '?')}): {msg}")
+        self.code = code
+
+
+class _Obs(ctypes.Structure):
+    _fields_ = [("T00", ctypes.c_double), ("electric", ctypes.c_double), ("magnetic", ctypes.c_double),
+                ("esqr", ctypes.c_double * 3), ("bsqr", ctypes.c_double * 3),
+                ("gauss_max", ctypes.c_double), ("gauss_rms", ctypes.c_double), ("gauss_absmax", ctypes.c_double),
+                ("unit_max", ctypes.c_double), ("unit_rms", ctypes.c_double),
+                ("edotb", ctypes.c_double), ("ncs_dot", ctypes.c_double), ("ncs", ctypes.c_double),
+                ("nonfinite", ctypes.c_int)]
+
+
+@dataclass
+class Observables:
+    T00: float
+    electric: float
+    magnetic: float
+    esqr: tuple
+    bsqr: tuple
+    gauss_max: float
+    gauss_rms: float
+    gauss_absmax: float
+    unit_max: float
+    unit_rms: float
+    edotb: float
+    ncs_dot: float
+    ncs: float
+    nonfinite: bool
+
+    def as_oracle_vector(self) -> np.ndarray:
+        """Same 16-slot order as the oracle's observables() output."""
+        v = np.zeros(16)
+        v[0], v[1], v[2] = self.T00, self.electric, self.magnetic
+        v[3:6], v[6:9] = self.esqr, self.bsqr
+        v[9], v[10], v[11], v[12], v[13] = self.gauss_max, self.gauss_rms, self.unit_max, self.unit_rms, self.edotb
+        v[15] = self.gauss_absmax
+        return v
+
+
+_LIB = None
+_dp = ctypes.POINTER(ctypes.c_double)
+
+
+def library() -> ctypes.CDLL:
+    """Load libtcym.so (building it if the toolkit is present and it is missing or stale)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = _build.LIB
+    if not os.path.exists(path) or os.environ.get("TCYM_REBUILD"):
+        _build.build_library()
+    L = ctypes.CDLL(path)
+    c_void_pp = ctypes.POINTER(ctypes.c_void_p)
+    sig = {
+        "tcym_version": ([], ctypes.c_int),
+        "tcym_ctx_create": ([ctypes.c_int, c_void_pp], ctypes.c_int),
+        "tcym_ctx_destroy": ([ctypes.c_void_p], ctypes.c_int),
+        "tcym_last_error": ([ctypes.c_void_p], ctypes.c_char_p),
+        "tcym_lattice_create": ([ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                 ctypes.c_int, c_void_pp], ctypes.c_int),
+        "tcym_lattice_create_ex": ([ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp,
+                                    ctypes.c_int, c_void_pp], ctypes.c_int),
+        "tcym_lattice_destroy": ([ctypes.c_void_p], ctypes.c_int),
+        "tcym_lattice_bytes": ([ctypes.c_void_p, ctypes.POINTER(ctypes.c_size_t)], ctypes.c_int),
+        "tcym_lattice_upload": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+        "tcym_lattice_download": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+        "tcym_lattice_copy": ([ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+        "tcym_lattice_sync": ([ctypes.c_void_p], ctypes.c_int),
+        "tcym_set_zero": ([ctypes.c_void_p], ctypes.c_int),
+        "tcym_gaussian_efield": ([ctypes.c_void_p, ctypes.c_double, ctypes.c_uint64], ctypes.c_int),
+        "tcym_random_links": ([ctypes.c_void_p, ctypes.c_double, ctypes.c_uint64], ctypes.c_int),
+        "tcym_gauss_restore": ([ctypes.c_void_p, ctypes.c_double, ctypes.c_int, ctypes.POINTER(ctypes.c_int), _dp],
+                               ctypes.c_int),
+        "tcym_leapfrog": ([ctypes.c_void_p, ctypes.c_double, ctypes.c_int], ctypes.c_int),
+        "tcym_update_e": ([ctypes.c_void_p, ctypes.c_double], ctypes.c_int),
+        "tcym_update_u": ([ctypes.c_void_p, ctypes.c_double], ctypes.c_int),
+        "tcym_langevin": ([ctypes.c_void_p, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_uint64,
+                           ctypes.c_uint64, ctypes.c_int], ctypes.c_int),
+        "tcym_flow": ([ctypes.c_void_p, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp], ctypes.c_int),
+        "tcym_reunitarize": ([ctypes.c_void_p], ctypes.c_int),
+        "tcym_set_reunitarize_period": ([ctypes.c_void_p, ctypes.c_int], ctypes.c_int),
+        "tcym_observables": ([ctypes.c_void_p, ctypes.POINTER(_Obs)], ctypes.c_int),
+        "tcym_edotb": ([ctypes.c_void_p, _dp], ctypes.c_int),
+        "tcym_ncs_track": ([ctypes.c_void_p, ctypes.c_int], ctypes.c_int),
+        "tcym_ncs_get": ([ctypes.c_void_p, _dp], ctypes.c_int),
+        "tcym_ncs_reset": ([ctypes.c_void_p], ctypes.c_int),
+    }
+    for name, (args, res) in sig.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = res
+    _LIB = L
+    return L
+
+
+def _ptr(a):
+    if a is None:
+        return None
+    assert a.dtype == np.float64 and a.flags.c_contiguous
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+class Context:
+    """A CUDA device opened by the library (tcym_ctx_create)."""
+
+    def __init__(self, device: int = 0):
+        self.lib = library()
+        h = ctypes.c_void_p()
+        rc = self.lib.tcym_ctx_create(device, ctypes.byref(h))
+        if rc != 0:
+            raise TcymError(rc, f"cannot open CUDA device {device}")
+        self.h = h
+
+    def check(self, rc: int) -> None:
+        if rc != 0:
+            msg = self.lib.tcym_last_error(self.h)
+            raise TcymError(rc, msg.decode() if msg else "")
+
+    def close(self) -> None:
+        if self.h:
+            self.lib.tcym_ctx_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+class Lattice:
+    """GaugeLinks + ElectricFields on the device (LATTICE/GaugeLinks.cpp, LATTICE/ElectricFields.cpp)."""
+
+    def __init__(self, ctx: Context, nc: int, shape, precision: int = FP64, spacing=None):
+        self.ctx, self.lib, self.nc = ctx, ctx.lib, nc
+        self.shape = tuple(int(n) for n in shape)
+        self.precision = precision
+        self.V = int(np.prod(self.shape))
+        h = ctypes.c_void_p()
+        if spacing is None:
+            rc = self.lib.tcym_lattice_create(ctx.h, nc, *self.shape, precision, ctypes.byref(h))
+        else:
+            a = (ctypes.c_double * 3)(*spacing)
+            rc = self.lib.tcym_lattice_create_ex(ctx.h, nc, *self.shape, a, precision, ctypes.byref(h))
+        ctx.check(rc)
+        self.h = h
+
+    def close(self):
+        if self.h:
+            self.lib.tcym_lattice_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ------------------------------------------------------------ state I/O
+    def upload(self, U=None, E=None):
+        self.ctx.check(self.lib.tcym_lattice_upload(self.h, _ptr(U), _ptr(E)))
+
+    def download(self):
+        U = np.empty((self.V, 3, NM[self.nc]))
+        E = np.empty((self.V, 3, NA[self.nc]))
+        self.ctx.check(self.lib.tcym_lattice_download(self.h, _ptr(U), _ptr(E)))
+        return U, E
+
+    def copy_from(self, other: "Lattice"):
+        self.ctx.check(self.lib.tcym_lattice_copy(self.h, other.h))
+
+    def nbytes(self) -> int:
+        n = ctypes.c_size_t()
+        self.ctx.check(self.lib.tcym_lattice_bytes(self.h, ctypes.byref(n)))
+        return n.value
+
+    def sync(self):
+        self.ctx.check(self.lib.tcym_lattice_sync(self.h))
+
+    # ---------------------------------------------------- initial conditions
+    def set_zero(self):
+        self.ctx.check(self.lib.tcym_set_zero(self.h))
+
+    def gaussian_efield(self, sigma: float, seed: int):
+        self.ctx.check(self.lib.tcym_gaussian_efield(self.h, sigma, seed))
+
+    def random_links(self, sigma: float, seed: int):
+        self.ctx.check(self.lib.tcym_random_links(self.h, sigma, seed))
+
+    def gauss_restore(self, tol: float = 1e-14, maxit: int = 10000):
+        it, mx = ctypes.c_int(), ctypes.c_double()
+        self.ctx.check(self.lib.tcym_gauss_restore(self.h, tol, maxit, ctypes.byref(it), ctypes.byref(mx)))
+        return it.value, mx.value
+
+    # -------------------------------------------------------------- dynamics
+    def leapfrog(self, dt: float, nsteps: int = 1):
+        self.ctx.check(self.lib.tcym_leapfrog(self.h, dt, nsteps))
+
+    def update_e(self, dt: float):
+        self.ctx.check(self.lib.tcym_update_e(self.h, dt))
+
+    def update_u(self, dt: float):
+        self.ctx.check(self.lib.tcym_update_u(self.h, dt))
+
+    def langevin(self, dt: float, gamma: float, T: float, seed: int, step0: int, nsteps: int = 1):
+        self.ctx.check(self.lib.tcym_langevin(self.h, dt, gamma, T, seed, step0, nsteps))
+
+    def flow(self, dtau: float, nsteps: int = 1, mode: int = FLOW_SIMULTANEOUS, calibrate: bool = False) -> float:
+        d = ctypes.c_double()
+        self.ctx.check(self.lib.tcym_flow(self.h, dtau, nsteps, mode, int(calibrate), ctypes.byref(d)))
+        return d.value
+
+    def reunitarize(self):
+        self.ctx.check(self.lib.tcym_reunitarize(self.h))
+
+    def set_reunitarize_period(self, period: int):
+        self.ctx.check(self.lib.tcym_set_reunitarize_period(self.h, period))
+
+    # ----------------------------------------------------------- observables
+    def observables(self, allow_nonfinite: bool = False) -> Observables:
+        o = _Obs()
+        rc = self.lib.tcym_observables(self.h, ctypes.byref(o))
+        if rc != 0 and not (allow_nonfinite and rc == 4):
+            self.ctx.check(rc)
+        return Observables(o.T00, o.electric, o.magnetic, tuple(o.esqr), tuple(o.bsqr), o.gauss_max, o.gauss_rms,
+                           o.gauss_absmax, o.unit_max, o.unit_rms, o.edotb, o.ncs_dot, o.ncs, bool(o.nonfinite))
+
+    def edotb(self) -> float:
+        d = ctypes.c_double()
+        self.ctx.check(self.lib.tcym_edotb(self.h, ctypes.byref(d)))
+        return d.value
+
+    def ncs_track(self, every: int = 1):
+        self.ctx.check(self.lib.tcym_ncs_track(self.h, every))
+
+    def ncs(self) -> float:
+        d = ctypes.c_double()
+        self.ctx.check(self.lib.tcym_ncs_get(self.h, ctypes.byref(d)))
+        return d.value
+
+    def ncs_reset(self):
+        self.ctx.check(self.lib.tcym_ncs_reset(self.h))

@@ -1,0 +1,562 @@
+// C ABI (include/tcym.h): contexts, lattice handles and the host side of
+// every call.  The host side only sizes launches and orders them on the
+// lattice's stream; all arithmetic is in the kernels.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <string>
+
+#include "../../include/tcym.h"
+#include "tcym_kernels.cuh"
+#include "tcym_internal.h"
+
+using namespace tcym;
+
+// ------------------------------------------------------------------ errors
+void tcym_set_error(tcym_ctx ctx, const char *fmt, ...) {
+    if (!ctx) return;
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    std::lock_guard<std::mutex> g(ctx->mu);
+    ctx->last_error = buf;
+}
+
+static int cuda_fail(tcym_ctx ctx, cudaError_t e, const char *where) {
+    tcym_set_error(ctx, "%s: %s", where, cudaGetErrorString(e));
+    return e == cudaErrorMemoryAllocation ? TCYM_ERR_OOM : TCYM_ERR_CUDA;
+}
+
+#define CK(call)                                                 \
+    do {                                                         \
+        cudaError_t e_ = (call);                                 \
+        if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call); \
+    } while (0)
+
+// ------------------------------------------------------- format dispatching
+// Runs `body` with the Launch<FMT> type of the lattice's storage format.
+#define DISPATCH(fmt, body)                                                \
+    switch (fmt) {                                                         \
+        case FMT_SU2_F32: { using L = Launch<FMT_SU2_F32>; body; } break;  \
+        case FMT_SU2_F64: { using L = Launch<FMT_SU2_F64>; body; } break;  \
+        case FMT_SU3_F32: { using L = Launch<FMT_SU3_F32>; body; } break;  \
+        case FMT_SU3_F64: { using L = Launch<FMT_SU3_F64>; body; } break;  \
+        default: return TCYM_ERR_ARG;                                      \
+    }
+
+int tcym_format_of(int nc, int precision) {
+    if (nc == 2) return precision == TCYM_FP32 ? FMT_SU2_F32 : FMT_SU2_F64;
+    return precision == TCYM_FP32 ? FMT_SU3_F32 : FMT_SU3_F64;
+}
+
+size_t tcym_link_bytes(int fmt) {
+    switch (fmt) {
+        case FMT_SU2_F32: return 16;
+        case FMT_SU2_F64: return 32;
+        case FMT_SU3_F32: return 48;
+        default: return 144;
+    }
+}
+size_t tcym_field_bytes(int fmt) {
+    switch (fmt) {
+        case FMT_SU2_F32: return 12;
+        case FMT_SU2_F64: return 24;
+        case FMT_SU3_F32: return 32;
+        default: return 64;
+    }
+}
+
+// Step coefficients of the reference for spacings a[3], Minkowski metric
+// (gUp = gDown = sqrt(-g) = 1, Dynamics.cpp:40-48) and aScale = 1.
+StepCoef<double> tcym_coef(const double *a, int mode, double dt, double gamma, double T, uint64_t seed,
+                           uint64_t step) {
+    StepCoef<double> c;
+    std::memset(&c, 0, sizeof(c));
+    c.mode = mode;
+    c.seed = seed;
+    c.step = step;
+    const double acube = a[0] * a[1] * a[2];
+    // leapfrog / Langevin: gamma = -2 dt sqrt(-g) a^3, cE = 1/a_mu^2 (Dynamics.cpp:150-155)
+    // flow: gamma = -2 sqrt(-g) a^3 aScale (GradientFlow.cpp:40-46)
+    const double g = mode == MODE_FLOW ? -2.0 * acube : -2.0 * dt * acube;
+    for (int mu = 0; mu < 3; ++mu) {
+        const double cE = 1.0 / (a[mu] * a[mu]);
+        c.fc[mu] = g * cE;
+        c.cnu[mu] = cE;
+        // cU = -dt gDown a_mu^2 / (sqrt(-g) a^3) (Dynamics.cpp:100-104; flow: dt -> DcTau, GradientFlow.cpp:111-115)
+        c.uc[mu] = -dt * a[mu] * a[mu] / acube;
+        if (mode == MODE_LANGEVIN) {
+            // cS = sqrt(-g) a^3 / a_mu^2 * dt, cR = sqrt(dt) / a_mu^2 (LangevinDynamics.cpp:182-188);
+            // xi = sqrt(2/beta) N(0,1) = sqrt(2T) N(0,1); damping gamma generalises the reference's 1
+            c.damp[mu] = gamma * acube * cE * dt;
+            c.kick[mu] = std::sqrt(gamma) * std::sqrt(dt) * cE * std::sqrt(2.0 * T);
+        }
+    }
+    return c;
+}
+
+// ------------------------------------------------------------------ context
+extern "C" int tcym_version(void) { return TCYM_VERSION; }
+
+extern "C" int tcym_ctx_create(int device, tcym_ctx *out) {
+    if (!out) return TCYM_ERR_ARG;
+    *out = nullptr;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || device < 0 || device >= n) return TCYM_ERR_CUDA;
+    tcym_ctx ctx = new (std::nothrow) tcym_ctx_s();
+    if (!ctx) return TCYM_ERR_OOM;
+    ctx->device = device;
+    if (cudaSetDevice(device) != cudaSuccess) { delete ctx; return TCYM_ERR_CUDA; }
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, device) == cudaSuccess) ctx->sm_count = prop.multiProcessorCount;
+    *out = ctx;
+    return TCYM_OK;
+}
+
+extern "C" int tcym_ctx_destroy(tcym_ctx ctx) {
+    if (!ctx) return TCYM_ERR_ARG;
+    delete ctx;
+    return TCYM_OK;
+}
+
+extern "C" const char *tcym_last_error(tcym_ctx ctx) {
+    if (!ctx) return "null context";
+    return ctx->last_error.c_str();
+}
+
+// ------------------------------------------------------------------ lattices
+static void lattice_free(tcym_lattice lat) {
+    cudaSetDevice(lat->ctx->device);
+    if (lat->stream) cudaStreamSynchronize(lat->stream);
+    cudaFree(lat->U[0]);
+    cudaFree(lat->U[1]);
+    cudaFree(lat->E);
+    cudaFree(lat->partial);
+    cudaFree(lat->result);
+    cudaFree(lat->gauss);
+    cudaFree(lat->staging);
+    if (lat->host_result) cudaFreeHost(lat->host_result);
+    if (lat->stream) cudaStreamDestroy(lat->stream);
+}
+
+extern "C" int tcym_lattice_create_ex(tcym_ctx ctx, int nc, int nx, int ny, int nz, const double a[3], int precision,
+                                      tcym_lattice *out) {
+    if (!ctx || !out) return TCYM_ERR_ARG;
+    *out = nullptr;
+    if ((nc != 2 && nc != 3) || (precision != TCYM_FP32 && precision != TCYM_FP64) || nx < 2 || ny < 2 || nz < 2) {
+        tcym_set_error(ctx, "tcym_lattice_create: nc must be 2 or 3, extents >= 2, precision FP32/FP64");
+        return TCYM_ERR_ARG;
+    }
+    const int64_t V = (int64_t)nx * ny * nz;
+    if (V >= (int64_t)1 << 32) {
+        tcym_set_error(ctx, "tcym_lattice_create: at most 2^32-1 sites (the noise counter holds a 32-bit site)");
+        return TCYM_ERR_ARG;
+    }
+    tcym_lattice lat = new (std::nothrow) tcym_lattice_s();
+    if (!lat) return TCYM_ERR_OOM;
+    lat->ctx = ctx;
+    lat->nc = nc;
+    lat->precision = precision;
+    lat->fmt = tcym_format_of(nc, precision);
+    lat->g = Geom{nx, ny, nz, V};
+    for (int i = 0; i < 3; ++i) lat->a[i] = a ? a[i] : 1.0;
+    lat->reunit_period = precision == TCYM_FP32 ? 100 : 0;
+    cudaSetDevice(ctx->device);
+    auto fail = [&](cudaError_t e, const char *w) {
+        int r = cuda_fail(ctx, e, w);
+        lattice_free(lat);
+        delete lat;
+        return r;
+    };
+    cudaError_t e;
+    if ((e = cudaStreamCreateWithFlags(&lat->stream, cudaStreamNonBlocking)) != cudaSuccess) return fail(e, "stream");
+    const size_t ub = 3 * tcym_link_bytes(lat->fmt) * (size_t)V, eb = 3 * tcym_field_bytes(lat->fmt) * (size_t)V;
+    if ((e = cudaMalloc(&lat->U[0], ub)) != cudaSuccess) return fail(e, "cudaMalloc(U)");
+    if ((e = cudaMalloc(&lat->U[1], ub)) != cudaSuccess) return fail(e, "cudaMalloc(U')");
+    if ((e = cudaMalloc(&lat->E, eb)) != cudaSuccess) return fail(e, "cudaMalloc(E)");
+    lat->max_blocks = ctx->sm_count * 8;
+    if ((e = cudaMalloc(&lat->partial, sizeof(double) * P_WIDTH * lat->max_blocks)) != cudaSuccess)
+        return fail(e, "cudaMalloc(partial)");
+    if ((e = cudaMalloc(&lat->result, sizeof(double) * R_WIDTH)) != cudaSuccess) return fail(e, "cudaMalloc(result)");
+    if ((e = cudaMemsetAsync(lat->result, 0, sizeof(double) * R_WIDTH, lat->stream)) != cudaSuccess)
+        return fail(e, "memset(result)");
+    if ((e = cudaMallocHost(&lat->host_result, sizeof(double) * R_WIDTH)) != cudaSuccess)
+        return fail(e, "cudaMallocHost(result)");
+    lat->bytes = 2 * ub + eb + sizeof(double) * (P_WIDTH * lat->max_blocks + R_WIDTH);
+    *out = lat;
+    return TCYM_OK;
+}
+
+extern "C" int tcym_lattice_create(tcym_ctx ctx, int nc, int nx, int ny, int nz, int precision, tcym_lattice *out) {
+    return tcym_lattice_create_ex(ctx, nc, nx, ny, nz, nullptr, precision, out);
+}
+
+extern "C" int tcym_lattice_destroy(tcym_lattice lat) {
+    if (!lat) return TCYM_ERR_ARG;
+    lattice_free(lat);
+    delete lat;
+    return TCYM_OK;
+}
+
+extern "C" int tcym_lattice_bytes(tcym_lattice lat, size_t *bytes) {
+    if (!lat || !bytes) return TCYM_ERR_ARG;
+    *bytes = lat->bytes + lat->staging_bytes + (lat->gauss ? sizeof(double) * 8 * (size_t)lat->g.V : 0);
+    return TCYM_OK;
+}
+
+static int ensure_staging(tcym_lattice lat) {
+    tcym_ctx ctx = lat->ctx;
+    const int nmd = lat->nc == 2 ? 4 : 18, na = lat->nc == 2 ? 3 : 8;
+    const size_t need = sizeof(double) * 3 * (size_t)(nmd + na) * (size_t)lat->g.V;
+    if (lat->staging_bytes >= need) return TCYM_OK;
+    cudaFree(lat->staging);
+    lat->staging = nullptr;
+    lat->staging_bytes = 0;
+    CK(cudaMalloc(&lat->staging, need));
+    lat->staging_bytes = need;
+    return TCYM_OK;
+}
+
+extern "C" int tcym_lattice_upload(tcym_lattice lat, const double *U_aos, const double *E_aos) {
+    if (!lat) return TCYM_ERR_ARG;
+    tcym_ctx ctx = lat->ctx;
+    cudaSetDevice(ctx->device);
+    int r = ensure_staging(lat);
+    if (r) return r;
+    const int nmd = lat->nc == 2 ? 4 : 18, na = lat->nc == 2 ? 3 : 8;
+    const size_t V = (size_t)lat->g.V;
+    double *du = lat->staging, *de = lat->staging + 3 * nmd * V;
+    if (U_aos) CK(cudaMemcpyAsync(du, U_aos, sizeof(double) * 3 * nmd * V, cudaMemcpyHostToDevice, lat->stream));
+    if (E_aos) CK(cudaMemcpyAsync(de, E_aos, sizeof(double) * 3 * na * V, cudaMemcpyHostToDevice, lat->stream));
+    DISPATCH(lat->fmt, CK(L::from_aos(lat->g, lat->U[lat->cur], lat->E, U_aos ? du : nullptr, E_aos ? de : nullptr,
+                                      lat->stream)));
+    CK(cudaStreamSynchronize(lat->stream));
+    return TCYM_OK;
+}
+
+extern "C" int tcym_lattice_download(tcym_lattice lat, double *U_aos, double *E_aos) {
+    if (!lat) return TCYM_ERR_ARG;
+    tcym_ctx ctx = lat->ctx;
+    cudaSetDevice(ctx->device);
+    int r = ensure_staging(lat);
+    if (r) return r;
+    const int nmd = lat->nc == 2 ? 4 : 18, na = lat->nc == 2 ? 3 : 8;
+    const size_t V = (size_t)lat->g.V;
+    double *du = lat->staging, *de = lat->staging + 3 * nmd * V;
+    DISPATCH(lat->fmt, CK(L::to_aos(lat->g, lat->U[lat->cur], lat->E, U_aos ? du : nullptr, E_aos ? de : nullptr,
+                                    lat->stream)));
+    if (U_aos) CK(cudaMemcpyAsync(U_aos, du, sizeof(double) * 3 * nmd * V, cudaMemcpyDeviceToHost, lat->stream));
+    if (E_aos) CK(cudaMemcpyAsync(E_aos, de, sizeof(double) * 3 * na * V, cudaMemcpyDeviceToHost, lat->stream));
+    CK(cudaStreamSynchronize(lat->stream));
+    return TCYM_OK;
+}
+
+extern "C" int tcym_lattice_copy(tcym_lattice dst, const tcym_lattice src) {
+    if (!dst || !src) return TCYM_ERR_ARG;
+    tcym_ctx ctx = dst->ctx;
+    if (dst->nc != src->nc || dst->g.nx != src->g.nx || dst->g.ny != src->g.ny || dst->g.nz != src->g.nz) {
+        tcym_set_error(ctx, "tcym_lattice_copy: group and extents must match");
+        return TCYM_ERR_ARG;
+    }
+    cudaSetDevice(ctx->device);
+    CK(cudaStreamSynchronize(src->stream));
+    if (dst->fmt == src->fmt) {
+        const size_t ub = 3 * tcym_link_bytes(dst->fmt) * (size_t)dst->g.V;
+        const size_t eb = 3 * tcym_field_bytes(dst->fmt) * (size_t)dst->g.V;
+        CK(cudaMemcpyAsync(dst->U[dst->cur], src->U[src->cur], ub, cudaMemcpyDeviceToDevice, dst->stream));
+        CK(cudaMemcpyAsync(dst->E, src->E, eb, cudaMemcpyDeviceToDevice, dst->stream));
+    } else {
+        // through FP64 AoS on the device
+        int r = ensure_staging(dst);
+        if (r) return r;
+        const int nmd = dst->nc == 2 ? 4 : 18;
+        double *du = dst->staging, *de = dst->staging + 3 * nmd * (size_t)dst->g.V;
+        DISPATCH(src->fmt, CK(L::to_aos(src->g, src->U[src->cur], src->E, du, de, dst->stream)));
+        DISPATCH(dst->fmt, CK(L::from_aos(dst->g, dst->U[dst->cur], dst->E, du, de, dst->stream)));
+    }
+    CK(cudaStreamSynchronize(dst->stream));
+    return TCYM_OK;
+}
+
+extern "C" int tcym_lattice_sync(tcym_lattice lat) {
+    if (!lat) return TCYM_ERR_ARG;
+    tcym_ctx ctx = lat->ctx;
+    CK(cudaStreamSynchronize(lat->stream));
+    return TCYM_OK;
+}
+
+// ------------------------------------------------------- initial conditions
+extern "C" int tcym_set_zero(tcym_lattice lat) {
+    if (!lat) return TCYM_ERR_ARG;
+    tcym_ctx ctx = lat->ctx;
+    cudaSetDevice(ctx->device);
+    DISPATCH(lat->fmt, CK(L::set_zero(lat->g, lat->U[lat->cur], lat->E, lat->stream)));
+    return TCYM_OK;
+}
+
+extern "C" int tcym_gaussian_efield(tcym_lattice lat, double sigma, uint64_t seed) {
+    if (!lat) return TCYM_ERR_ARG;
+    tcym_ctx ctx = lat->ctx;
+    cudaSetDevice(ctx->device);
+    DISPATCH(lat->fmt, CK(L::gaussian_efield(lat->g, lat->E, sigma, seed, lat->stream)));
+    return TCYM_OK;
+}
+
+extern "C" int tcym_random_links(tcym_lattice lat, double sigma, uint64_t seed) {
+    if (!lat) return TCYM_ERR_ARG;
+    tcym_ctx ctx = lat->ctx;
+    cudaSetDevice(ctx->device);
+    DISPATCH(lat->fmt, CK(L::random_links(lat->g, lat->U[lat->cur], sigma, seed, lat->stream)));
+    return TCYM_OK;
+}
+
+// Runs the observables reduction with `mask` and the finaliser; result on device.
+int tcym_reduce(tcym_lattice lat, int mask, double ncs_dt) {
+    tcym_ctx ctx = lat->ctx;
+    int blocks = 0;
+    DISPATCH(lat->fmt, {
+        blocks = L::reduce_grid(lat->g, lat->max_blocks);
+        CK(L::observables(lat->g, lat->U[lat->cur], lat->E, mask, lat->partial, blocks, lat->stream));
+    });
+    CK(finalize_obs(lat->partial, blocks, lat->nc == 2 ? 3 : 8, lat->g.V, ncs_dt, lat->result, lat->stream));
+    return TCYM_OK;
+}
+
+static int fetch_result(tcym_lattice lat) {
+    tcym_ctx ctx = lat->ctx;
+    CK(cudaMemcpyAsync(lat->host_result, lat->result, sizeof(double) * R_WIDTH, cudaMemcpyDeviceToHost, lat->stream));
+    CK(cudaStreamSynchronize(lat->stream));
+    return TCYM_OK;
+}
+
+extern "C" int tcym_gauss_restore(tcym_lattice lat, double tol, int maxit, int *iters, double *final_max) {
+    if (!lat || maxit < 0) return TCYM_ERR_ARG;
+    tcym_ctx ctx = lat->ctx;
+    cudaSetDevice(ctx->device);
+    const int na = lat->nc == 2 ? 3 : 8;
+    if (!lat->gauss) CK(cudaMalloc(&lat->gauss, sizeof(double) * na * (size_t)lat->g.V));
+    const double gam[3] = {7.0 / 24.0, 7.0 / 48.0, 7.0 / 72.0};
+    int blocks = 0;
+    DISPATCH(lat->fmt, blocks = L::reduce_grid(lat->g, lat->max_blocks));
+    auto deviation = [&]() -> int {
+        DISPATCH(lat->fmt, CK(L::gauss_compute(lat->g, lat->U[lat->cur], lat->E, lat->gauss, lat->partial, blocks,
+                                               lat->stream)));
+        CK(finalize_obs(lat->partial, blocks, na, lat->g.V, 0.0, lat->result, lat->stream));
+        return TCYM_OK;
+    };
+    // initial deviation (GaussRestore.cpp:143)
+    int r = deviation();
+    if (r) return r;
+    if ((r = fetch_result(lat))) return r;
+    double gmax = lat->host_result[R_GMAX];
+    int it = 0;
+    while (it < maxit && gmax > tol) {
+        for (int k = 0; k < 3; ++k) {
+            if ((r = deviation())) return r;
+            DISPATCH(lat->fmt,
+                     CK(L::gauss_update(lat->g, lat->U[lat->cur], lat->E, lat->gauss, gam[k], lat->stream)));
+        }
+        if ((r = fetch_result(lat))) return r;  // max of the last deviation, as the reference tests it
+        gmax = lat->host_result[R_GMAX];
+        if (!std::isfinite(gmax)) {
+            tcym_set_error(ctx, "tcym_gauss_restore: non-finite violation at iteration %d", it);
+            return TCYM_ERR_NONFINITE;
+        }
+        ++it;
+    }
+    if (iters) *iters = it;
+    if (final_max) *final_max = gmax;
+    return TCYM_OK;
+}
+
+// ------------------------------------------------------------------ dynamics
+static int maybe_track(tcym_lattice lat, double dt, int64_t step_index) {
+    if (lat->ncs_every > 0 && (step_index % lat->ncs_every) == 0)
+        return tcym_reduce(lat, OBS_EDOTB, dt * lat->ncs_every);
+    return TCYM_OK;
+}
+
+static int maybe_reunitarize(tcym_lattice lat) {
+    tcym_ctx ctx = lat->ctx;
+    ++lat->steps_since_reunit;
+    if (lat->reunit_period > 0 && lat->steps_since_reunit >= lat->reunit_period) {
+        DISPATCH(lat->fmt, CK(L::reunitarize(lat->g, lat->U[lat->cur], lat->stream)));
+        lat->steps_since_reunit = 0;
+    }
+    return TCYM_OK;
+}
+
+int tcym_run_steps(tcym_lattice lat, int mode, double dt, double gamma, double T, uint64_t seed, uint64_t step0,
+                   int nsteps) {
+    tcym_ctx ctx = lat->ctx;
+    cudaSetDevice(ctx->device);
+    for (int i = 0; i < nsteps; ++i) {
+        StepCoef<double> c = tcym_coef(lat->a, mode, dt, gamma, T, seed, step0 + (uint64_t)i);
+        DISPATCH(lat->fmt,
+                 CK(L::step(lat->g, lat->U[lat->cur], lat->U[1 - lat->cur], lat->E, c, true, true, lat->stream)));
+        lat->cur ^= 1;
+        ++lat->steps_done;
+        int r = maybe_reunitarize(lat);
+        if (r) return r;
+        if ((r = maybe_track(lat, dt, lat->steps_done))) return r;
+    }
+    return TCYM_OK;
+}
+
+extern "C" int tcym_leapfrog(tcym_lattice lat, double dt, int nsteps) {
+    if (!lat || nsteps < 0) return TCYM_ERR_ARG;
+    return tcym_run_steps(lat, MODE_LEAPFROG, dt, 0, 0, 0, 0, nsteps);
+}
+
+extern "C" int tcym_langevin(tcym_lattice lat, double dt, double gamma, double T, uint64_t seed, uint64_t step0,
+                             int nsteps) {
+    if (!lat || nsteps < 0 || gamma < 0 || T < 0 || dt < 0) return TCYM_ERR_ARG;
+    return tcym_run_steps(lat, MODE_LANGEVIN, dt, gamma, T, seed, step0, nsteps);
+}
+
+extern "C" int tcym_update_e(tcym_lattice lat, double dt) {
+    if (!lat) return TCYM_ERR_ARG;
+    tcym_ctx ctx = lat->ctx;
+    cudaSetDevice(ctx->device);
+    StepCoef<double> c = tcym_coef(lat->a, MODE_LEAPFROG, dt, 0, 0, 0, 0);
+    DISPATCH(lat->fmt, CK(L::step(lat->g, lat->U[lat->cur], lat->U[lat->cur], lat->E, c, true, false, lat->stream)));
+    return TCYM_OK;
+}
+
+extern "C" int tcym_update_u(tcym_lattice lat, double dt) {
+    if (!lat) return TCYM_ERR_ARG;
+    tcym_ctx ctx = lat->ctx;
+    cudaSetDevice(ctx->device);
+    StepCoef<double> c = tcym_coef(lat->a, MODE_LEAPFROG, dt, 0, 0, 0, 0);
+    DISPATCH(lat->fmt, CK(L::step(lat->g, lat->U[lat->cur], lat->U[lat->cur], lat->E, c, false, true, lat->stream)));
+    return TCYM_OK;
+}
+
+extern "C" int tcym_flow(tcym_lattice lat, double dtau, int nsteps, int mode, int calibrate, double *dncs) {
+    if (!lat || nsteps < 0 || (mode != TCYM_FLOW_SIMULTANEOUS && mode != TCYM_FLOW_CHECKERBOARD)) return TCYM_ERR_ARG;
+    tcym_ctx ctx = lat->ctx;
+    cudaSetDevice(ctx->device);
+    if (mode == TCYM_FLOW_CHECKERBOARD && ((lat->g.nx | lat->g.ny | lat->g.nz) & 1)) {
+        tcym_set_error(ctx, "tcym_flow: checkerboard sweeps need even extents");
+        return TCYM_ERR_ARG;
+    }
+    const double inv8pi2 = 0.125 / (M_PI * M_PI);
+    double acc = 0.0;
+    StepCoef<double> c = tcym_coef(lat->a, MODE_FLOW, dtau, 0, 0, 0, 0);
+    int r;
+    for (int s = 0; s < nsteps; ++s) {
+        if (mode == TCYM_FLOW_SIMULTANEOUS) {
+            // F into E and U' = exp(-i dtau F) U into the other buffer; U stays intact
+            DISPATCH(lat->fmt, CK(L::step(lat->g, lat->U[lat->cur], lat->U[1 - lat->cur], lat->E, c, true, true,
+                                          lat->stream)));
+        } else {
+            if (calibrate)  // the force of the state before the sweep, for the trapezoid rule
+                DISPATCH(lat->fmt, CK(L::step(lat->g, lat->U[lat->cur], lat->U[lat->cur], lat->E, c, true, false,
+                                              lat->stream)));
+        }
+        if (calibrate) {
+            if ((r = tcym_reduce(lat, OBS_EDOTB, 0.0))) return r;
+            if ((r = fetch_result(lat))) return r;
+            acc += 0.5 * dtau * inv8pi2 * lat->host_result[R_EDB];
+        }
+        if (mode == TCYM_FLOW_SIMULTANEOUS) {
+            lat->cur ^= 1;
+        } else {
+            for (int p = 0; p < 2; ++p)
+                for (int mu = 0; mu < 3; ++mu)
+                    DISPATCH(lat->fmt, CK(L::flow_cb(lat->g, lat->U[lat->cur], p, mu, c.fc, c.cnu, c.uc, lat->stream)));
+        }
+        if (calibrate) {
+            if ((r = tcym_reduce(lat, OBS_EDOTB, 0.0))) return r;
+            if ((r = fetch_result(lat))) return r;
+            acc += 0.5 * dtau * inv8pi2 * lat->host_result[R_EDB];
+        }
+    }
+    if (dncs) *dncs = acc;
+    return TCYM_OK;
+}
+
+extern "C" int tcym_reunitarize(tcym_lattice lat) {
+    if (!lat) return TCYM_ERR_ARG;
+    tcym_ctx ctx = lat->ctx;
+    cudaSetDevice(ctx->device);
+    DISPATCH(lat->fmt, CK(L::reunitarize(lat->g, lat->U[lat->cur], lat->stream)));
+    lat->steps_since_reunit = 0;
+    return TCYM_OK;
+}
+
+extern "C" int tcym_set_reunitarize_period(tcym_lattice lat, int period) {
+    if (!lat || period < 0) return TCYM_ERR_ARG;
+    lat->reunit_period = period;
+    lat->steps_since_reunit = 0;
+    return TCYM_OK;
+}
+
+// ---------------------------------------------------------------- observables
+extern "C" int tcym_observables(tcym_lattice lat, tcym_obs *out) {
+    if (!lat || !out) return TCYM_ERR_ARG;
+    cudaSetDevice(lat->ctx->device);
+    int r = tcym_reduce(lat, OBS_ALL, 0.0);
+    if (r) return r;
+    if ((r = fetch_result(lat))) return r;
+    const double *h = lat->host_result;
+    std::memset(out, 0, sizeof(*out));
+    for (int m = 0; m < 3; ++m) { out->esqr[m] = h[R_ESQ0 + m]; out->bsqr[m] = h[R_BSQ0 + m]; }
+    // Bulk::ELECTRIC/MAGNETIC/T00 with cE = cB = 1 (BulkObservables.cpp:17-51)
+    out->electric = 0.5 * (out->esqr[0] + out->esqr[1] + out->esqr[2]);
+    out->magnetic = 0.5 * (out->bsqr[0] + out->bsqr[1] + out->bsqr[2]);
+    out->T00 = out->electric + out->magnetic;
+    out->gauss_max = h[R_GMAX];
+    out->gauss_rms = h[R_GRMS];
+    out->gauss_absmax = h[R_GABS];
+    out->unit_max = h[R_UMAX];
+    out->unit_rms = h[R_URMS];
+    out->edotb = h[R_EDB];
+    out->ncs_dot = 0.125 * out->edotb / (M_PI * M_PI);
+    out->ncs = h[R_NCS];
+    out->nonfinite = h[R_NONFINITE] != 0.0;
+    if (out->nonfinite) {
+        tcym_set_error(lat->ctx, "tcym_observables: non-finite reduction");
+        return TCYM_ERR_NONFINITE;
+    }
+    return TCYM_OK;
+}
+
+extern "C" int tcym_edotb(tcym_lattice lat, double *out) {
+    if (!lat || !out) return TCYM_ERR_ARG;
+    cudaSetDevice(lat->ctx->device);
+    int r = tcym_reduce(lat, OBS_EDOTB, 0.0);
+    if (r) return r;
+    if ((r = fetch_result(lat))) return r;
+    *out = lat->host_result[R_EDB];
+    return TCYM_OK;
+}
+
+extern "C" int tcym_ncs_track(tcym_lattice lat, int every) {
+    if (!lat || every < 0) return TCYM_ERR_ARG;
+    lat->ncs_every = every;
+    return TCYM_OK;
+}
+
+extern "C" int tcym_ncs_get(tcym_lattice lat, double *ncs) {
+    if (!lat || !ncs) return TCYM_ERR_ARG;
+    int r = fetch_result(lat);
+    if (r) return r;
+    *ncs = lat->host_result[R_NCS];
+    return TCYM_OK;
+}
+
+extern "C" int tcym_ncs_reset(tcym_lattice lat) {
+    if (!lat) return TCYM_ERR_ARG;
+    tcym_ctx ctx = lat->ctx;
+    CK(cudaMemsetAsync(lat->result + R_NCS, 0, 2 * sizeof(double), lat->stream));
+    CK(cudaStreamSynchronize(lat->stream));
+    return TCYM_OK;
+}

@@ -1,0 +1,49 @@
+// Internal state behind the opaque handles of include/tcym.h.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <mutex>
+#include <string>
+
+#include "../../include/tcym.h"
+#include "tcym_site.cuh"
+
+struct tcym_ctx_s {
+    int device = 0;
+    int sm_count = 152;
+    std::mutex mu;
+    std::string last_error;
+};
+
+struct tcym_lattice_s {
+    tcym_ctx ctx = nullptr;
+    int nc = 0, precision = 0, fmt = 0;
+    tcym::Geom g{};
+    double a[3] = {1, 1, 1};
+    void *U[2] = {nullptr, nullptr};  // ping-pong link buffers; U[cur] is the state
+    int cur = 0;
+    void *E = nullptr;
+    double *partial = nullptr;  // per-block reduction records
+    int max_blocks = 0;
+    double *result = nullptr;   // device result block (also holds the Kahan N_CS)
+    double *host_result = nullptr;
+    double *gauss = nullptr;    // Gauss violation scratch, allocated by the first restore
+    double *staging = nullptr;  // AoS FP64 staging for upload/download, allocated on first use
+    size_t staging_bytes = 0;
+    size_t bytes = 0;
+    cudaStream_t stream = nullptr;
+    int reunit_period = 0, steps_since_reunit = 0;
+    int ncs_every = 0;
+    int64_t steps_done = 0;
+};
+
+void tcym_set_error(tcym_ctx ctx, const char *fmt, ...);
+int tcym_format_of(int nc, int precision);
+size_t tcym_link_bytes(int fmt);
+size_t tcym_field_bytes(int fmt);
+tcym::StepCoef<double> tcym_coef(const double *a, int mode, double dt, double gamma, double T, uint64_t seed,
+                                 uint64_t step);
+int tcym_reduce(tcym_lattice lat, int mask, double ncs_dt);
+int tcym_run_steps(tcym_lattice lat, int mode, double dt, double gamma, double T, uint64_t seed, uint64_t step0,
+                   int nsteps);

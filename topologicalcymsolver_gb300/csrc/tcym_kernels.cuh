@@ -1,0 +1,258 @@
+// CUDA kernels and their launchers, one instantiation per storage format
+// (tcym_kern_su2.cu, tcym_kern_su3.cu).
+//
+// Every kernel is one thread per site (or per link for the checkerboard
+// flow), grid-strided over the lattice.  Reductions are deterministic: each
+// block writes one partial record (FP64) and a single-block finaliser sums the
+// partials in block order, so a result never depends on scheduling.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "tcym_site.cuh"
+
+namespace tcym {
+
+// partial record of one block: 9 sums and 3 maxima
+enum : int {
+    P_ESQ0 = 0, P_BSQ0 = 3, P_GSQ = 6, P_USQ = 7, P_EDB = 8, P_GMAX = 9, P_GABS = 10, P_UMAX = 11, P_WIDTH = 12
+};
+// device result block (doubles), written by finalize_obs
+enum : int {
+    R_ESQ0 = 0, R_BSQ0 = 3, R_GMAX = 6, R_GRMS = 7, R_GABS = 8, R_UMAX = 9, R_URMS = 10, R_EDB = 11,
+    R_NCS = 12, R_NCS_COMP = 13, R_NONFINITE = 14, R_WIDTH = 16
+};
+
+constexpr int kThreadsSU2 = 256;
+constexpr int kThreadsSU3 = 128;
+constexpr int kRedThreads = 256;
+
+template <int FMT> constexpr int threads_for() { return Fmt<FMT>::NA == 3 ? kThreadsSU2 : kThreadsSU3; }
+
+inline int grid_for(int64_t n, int threads) {
+    int64_t b = (n + threads - 1) / threads;
+    return (int)(b < 1 ? 1 : b);
+}
+
+template <class T> StepCoef<T> coef_cast(const StepCoef<double> &c) {
+    StepCoef<T> r;
+    r.mode = c.mode;
+    r.seed = c.seed;
+    r.step = c.step;
+    for (int i = 0; i < 3; ++i) {
+        r.fc[i] = (T)c.fc[i]; r.cnu[i] = (T)c.cnu[i]; r.uc[i] = (T)c.uc[i];
+        r.damp[i] = (T)c.damp[i]; r.kick[i] = (T)c.kick[i];
+    }
+    return r;
+}
+
+// ------------------------------------------------------------------ kernels
+template <int FMT, bool DO_E, bool DO_U>
+__global__ void __launch_bounds__(threads_for<FMT>()) k_step(Geom g, const void *Uin, void *Uout, void *E,
+                                                             StepCoef<typename Fmt<FMT>::T> c) {
+    int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= g.V) return;
+    site_step<Fmt<FMT>, DO_E, DO_U>(g, Uin, Uout, E, c, s);
+}
+
+// sites of parity p, for even extents: t -> (x, row) with x of the right parity
+template <int FMT>
+__global__ void __launch_bounds__(threads_for<FMT>()) k_flow_cb(Geom g, void *U, int parity, int mu,
+                                                                typename Fmt<FMT>::T fc0, typename Fmt<FMT>::T fc1,
+                                                                typename Fmt<FMT>::T fc2, typename Fmt<FMT>::T cn0,
+                                                                typename Fmt<FMT>::T cn1, typename Fmt<FMT>::T cn2,
+                                                                typename Fmt<FMT>::T uc0, typename Fmt<FMT>::T uc1,
+                                                                typename Fmt<FMT>::T uc2) {
+    using T = typename Fmt<FMT>::T;
+    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= g.V / 2) return;
+    const int hx = g.nx / 2;
+    int64_t row = t / hx;
+    int xh = (int)(t - row * hx);
+    int y = (int)(row % g.ny), z = (int)(row / g.ny);
+    int x = 2 * xh + ((y + z + parity) & 1);
+    int64_t s = x + (int64_t)g.nx * row;
+    const T fc[3] = {fc0, fc1, fc2}, cn[3] = {cn0, cn1, cn2}, uc[3] = {uc0, uc1, uc2};
+    link_flow<Fmt<FMT>>(g, U, mu, fc, cn, uc, s);
+}
+
+// block reduction helpers (FP64)
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ double warp_max(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+// Reduce vals[0..P_WIDTH) over the block into partial[blockIdx.x * P_WIDTH ..].
+__device__ __forceinline__ void block_partial(double *vals, double *partial) {
+    __shared__ double sh[32][P_WIDTH];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+    for (int k = 0; k < P_WIDTH; ++k) vals[k] = k < P_GMAX ? warp_sum(vals[k]) : warp_max(vals[k]);
+    if (lane == 0)
+#pragma unroll
+        for (int k = 0; k < P_WIDTH; ++k) sh[w][k] = vals[k];
+    __syncthreads();
+    if (threadIdx.x < P_WIDTH) {
+        const int k = threadIdx.x;
+        double r = sh[0][k];
+        for (int i = 1; i < nw; ++i) r = k < P_GMAX ? r + sh[i][k] : fmax(r, sh[i][k]);
+        partial[(int64_t)blockIdx.x * P_WIDTH + k] = r;
+    }
+}
+
+template <int FMT>
+__global__ void __launch_bounds__(kRedThreads) k_observables(Geom g, const void *U, const void *E, int mask,
+                                                             double *partial) {
+    using F = Fmt<FMT>;
+    double v[P_WIDTH];
+#pragma unroll
+    for (int k = 0; k < P_WIDTH; ++k) v[k] = 0.0;
+    v[P_GMAX] = 0.0;  // signed maximum starts at 0 (GaussLawViolation.cpp:17,44)
+    for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < g.V; s += (int64_t)gridDim.x * blockDim.x) {
+        SiteObs<F> o;
+        site_observables<F>(g, U, E, mask, s, o);
+        for (int m = 0; m < 3; ++m) { v[P_ESQ0 + m] += o.esq[m]; v[P_BSQ0 + m] += o.bsq[m]; }
+        for (int a = 0; a < F::NA; ++a) {
+            v[P_GSQ] += o.g[a] * o.g[a];
+            v[P_GMAX] = fmax(v[P_GMAX], o.g[a]);
+            v[P_GABS] = fmax(v[P_GABS], fabs(o.g[a]));
+        }
+        for (int m = 0; m < 3; ++m) { v[P_USQ] += o.un[m] * o.un[m]; v[P_UMAX] = fmax(v[P_UMAX], o.un[m]); }
+        v[P_EDB] += o.edotb;
+    }
+    block_partial(v, partial);
+}
+
+// Gauss violation into the FP64 scratch G[a*V + s]; partial maxima as for observables.
+template <int FMT>
+__global__ void __launch_bounds__(kRedThreads) k_gauss_compute(Geom g, const void *U, const void *E, double *G,
+                                                               double *partial) {
+    using F = Fmt<FMT>;
+    double v[P_WIDTH];
+#pragma unroll
+    for (int k = 0; k < P_WIDTH; ++k) v[k] = 0.0;
+    for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < g.V; s += (int64_t)gridDim.x * blockDim.x) {
+        double gv[F::NA];
+        site_gauss<F>(g, U, E, s, gv);
+        for (int a = 0; a < F::NA; ++a) {
+            G[a * g.V + s] = gv[a];
+            v[P_GSQ] += gv[a] * gv[a];
+            v[P_GMAX] = fmax(v[P_GMAX], gv[a]);
+            v[P_GABS] = fmax(v[P_GABS], fabs(gv[a]));
+        }
+    }
+    block_partial(v, partial);
+}
+
+template <int FMT>
+__global__ void __launch_bounds__(threads_for<FMT>()) k_gauss_update(Geom g, const void *U, void *E, const double *G,
+                                                                     double gam) {
+    int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= g.V) return;
+    site_gauss_update<Fmt<FMT>>(g, U, E, G, gam, s);
+}
+
+template <int FMT> __global__ void k_set_zero(Geom g, void *U, void *E) {
+    int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < g.V) site_set_zero<Fmt<FMT>>(g, U, E, s);
+}
+template <int FMT> __global__ void k_gaussian_efield(Geom g, void *E, double sigma, uint64_t seed) {
+    int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < g.V) site_gaussian_efield<Fmt<FMT>>(g, E, sigma, seed, s);
+}
+template <int FMT> __global__ void k_random_links(Geom g, void *U, double sigma, uint64_t seed) {
+    int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < g.V) site_random_links<Fmt<FMT>>(g, U, sigma, seed, s);
+}
+template <int FMT> __global__ void k_reunitarize(Geom g, void *U) {
+    int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < g.V) site_reunitarize<Fmt<FMT>>(g, U, s);
+}
+template <int FMT> __global__ void k_from_aos(Geom g, void *U, void *E, const double *Ua, const double *Ea) {
+    int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < g.V) site_from_aos<Fmt<FMT>>(g, U, E, Ua, Ea, s);
+}
+template <int FMT> __global__ void k_to_aos(Geom g, const void *U, const void *E, double *Ua, double *Ea) {
+    int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < g.V) site_to_aos<Fmt<FMT>>(g, U, E, Ua, Ea, s);
+}
+
+// ------------------------------------------------------------------ launchers
+template <int FMT> struct Launch {
+    using F = Fmt<FMT>;
+    using T = typename F::T;
+    static constexpr int TPB = threads_for<FMT>();
+
+    static cudaError_t step(const Geom &g, const void *Uin, void *Uout, void *E, const StepCoef<double> &cd, bool doE,
+                            bool doU, cudaStream_t st) {
+        StepCoef<T> c = coef_cast<T>(cd);
+        int grid = grid_for(g.V, TPB);
+        if (doE && doU) k_step<FMT, true, true><<<grid, TPB, 0, st>>>(g, Uin, Uout, E, c);
+        else if (doE) k_step<FMT, true, false><<<grid, TPB, 0, st>>>(g, Uin, Uout, E, c);
+        else k_step<FMT, false, true><<<grid, TPB, 0, st>>>(g, Uin, Uout, E, c);
+        return cudaGetLastError();
+    }
+    static cudaError_t flow_cb(const Geom &g, void *U, int parity, int mu, const double *fc, const double *cn,
+                               const double *uc, cudaStream_t st) {
+        int grid = grid_for(g.V / 2, TPB);
+        k_flow_cb<FMT><<<grid, TPB, 0, st>>>(g, U, parity, mu, (T)fc[0], (T)fc[1], (T)fc[2], (T)cn[0], (T)cn[1],
+                                             (T)cn[2], (T)uc[0], (T)uc[1], (T)uc[2]);
+        return cudaGetLastError();
+    }
+    static int reduce_grid(const Geom &g, int max_blocks) {
+        int b = grid_for(g.V, kRedThreads);
+        return b < max_blocks ? b : max_blocks;
+    }
+    static cudaError_t observables(const Geom &g, const void *U, const void *E, int mask, double *partial, int blocks,
+                                   cudaStream_t st) {
+        k_observables<FMT><<<blocks, kRedThreads, 0, st>>>(g, U, E, mask, partial);
+        return cudaGetLastError();
+    }
+    static cudaError_t gauss_compute(const Geom &g, const void *U, const void *E, double *G, double *partial,
+                                     int blocks, cudaStream_t st) {
+        k_gauss_compute<FMT><<<blocks, kRedThreads, 0, st>>>(g, U, E, G, partial);
+        return cudaGetLastError();
+    }
+    static cudaError_t gauss_update(const Geom &g, const void *U, void *E, const double *G, double gam,
+                                    cudaStream_t st) {
+        k_gauss_update<FMT><<<grid_for(g.V, TPB), TPB, 0, st>>>(g, U, E, G, gam);
+        return cudaGetLastError();
+    }
+    static cudaError_t set_zero(const Geom &g, void *U, void *E, cudaStream_t st) {
+        k_set_zero<FMT><<<grid_for(g.V, 256), 256, 0, st>>>(g, U, E);
+        return cudaGetLastError();
+    }
+    static cudaError_t gaussian_efield(const Geom &g, void *E, double sigma, uint64_t seed, cudaStream_t st) {
+        k_gaussian_efield<FMT><<<grid_for(g.V, 128), 128, 0, st>>>(g, E, sigma, seed);
+        return cudaGetLastError();
+    }
+    static cudaError_t random_links(const Geom &g, void *U, double sigma, uint64_t seed, cudaStream_t st) {
+        k_random_links<FMT><<<grid_for(g.V, 128), 128, 0, st>>>(g, U, sigma, seed);
+        return cudaGetLastError();
+    }
+    static cudaError_t reunitarize(const Geom &g, void *U, cudaStream_t st) {
+        k_reunitarize<FMT><<<grid_for(g.V, 128), 128, 0, st>>>(g, U);
+        return cudaGetLastError();
+    }
+    static cudaError_t from_aos(const Geom &g, void *U, void *E, const double *Ua, const double *Ea, cudaStream_t st) {
+        k_from_aos<FMT><<<grid_for(g.V, 128), 128, 0, st>>>(g, U, E, Ua, Ea);
+        return cudaGetLastError();
+    }
+    static cudaError_t to_aos(const Geom &g, const void *U, const void *E, double *Ua, double *Ea, cudaStream_t st) {
+        k_to_aos<FMT><<<grid_for(g.V, 128), 128, 0, st>>>(g, U, E, Ua, Ea);
+        return cudaGetLastError();
+    }
+};
+
+// Sum the block partials in block order and write the result block; optionally
+// advance the Kahan-compensated N_CS by ncs_dt * E.B / (8 pi^2).
+cudaError_t finalize_obs(const double *partial, int blocks, int na, int64_t V, double ncs_dt, double *result,
+                         cudaStream_t st);
+
+}  // namespace tcym

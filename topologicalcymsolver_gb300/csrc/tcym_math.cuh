@@ -1,0 +1,415 @@
+// Group and algebra arithmetic for SU(2) and SU(3) links, shared by every kernel.
+//
+// All functions are __host__ __device__ so the same per-site code that the
+// CUDA kernels run can also be instantiated on the host by the test-only
+// build (tcym_hostcheck.cu) and compared with the FP64 oracle without a GPU.
+//
+// Conventions (those of the reference, SUNc/):
+//   SU(2): U = u3*1 + i u_k sigma_k, four reals (SU2/GroupOperations.cpp:4-14)
+//   SU(3): 3x3 complex; generators t^a = lambda^a/2 (SU3/AlgebraOperations.cpp:6-7)
+//   proj(V)^a = Re tr(i t^a V)  (ReTrIGenU: SU2/GroupOperations.cpp:78-84,
+//                                SU3/GroupOperations.cpp:108-118)
+//   iexp(c, e) = exp(i c t^a e^a) (MatrixIExp: SU2/AlgebraOperations.cpp:37-55,
+//                                  SU3/AlgebraOperations.cpp:141-182)
+// The SU(3) exponential here is not the reference's eigen-decomposition: it
+// reduces the Taylor series of exp(iQ) with the Cayley-Hamilton identity
+// Q^3 = c1 Q + c0 (traceless Hermitian Q, c1 = tr Q^2 / 2, c0 = det Q), so that
+// exp(iQ) = f0 + f1 Q + f2 Q^2 with real-coefficient scalar recurrences only,
+// after scaling Q by 2^-k until its spectral radius is <= 1/2 and squaring back.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#define TCYM_HD __host__ __device__ __forceinline__
+
+namespace tcym {
+
+// ------------------------------------------------------------------ scalars
+template <class T> struct Real;
+template <> struct Real<float> {
+    static TCYM_HD float sqrt_(float x) { return sqrtf(x); }
+    static TCYM_HD float rsqrt_(float x) {
+#ifdef __CUDA_ARCH__
+        return rsqrtf(x);
+#else
+        return 1.0f / sqrtf(x);
+#endif
+    }
+    static TCYM_HD float log_(float x) { return logf(x); }
+    static TCYM_HD void sincos_(float x, float *s, float *c) {
+#ifdef __CUDA_ARCH__
+        sincosf(x, s, c);
+#else
+        *s = sinf(x); *c = cosf(x);
+#endif
+    }
+    // sin(pi x), cos(pi x)
+    static TCYM_HD void sincospi_(float x, float *s, float *c) {
+#ifdef __CUDA_ARCH__
+        sincospif(x, s, c);
+#else
+        *s = (float)sin(3.14159265358979323846 * (double)x);
+        *c = (float)cos(3.14159265358979323846 * (double)x);
+#endif
+    }
+};
+template <> struct Real<double> {
+    static TCYM_HD double sqrt_(double x) { return sqrt(x); }
+    static TCYM_HD double rsqrt_(double x) { return 1.0 / sqrt(x); }
+    static TCYM_HD double log_(double x) { return log(x); }
+    static TCYM_HD void sincos_(double x, double *s, double *c) {
+#ifdef __CUDA_ARCH__
+        sincos(x, s, c);
+#else
+        *s = sin(x); *c = cos(x);
+#endif
+    }
+    static TCYM_HD void sincospi_(double x, double *s, double *c) {
+#ifdef __CUDA_ARCH__
+        sincospi(x, s, c);
+#else
+        *s = sin(3.14159265358979323846264338327950288 * x);
+        *c = cos(3.14159265358979323846264338327950288 * x);
+#endif
+    }
+};
+
+template <class T> struct cx {
+    T re, im;
+};
+template <class T> TCYM_HD cx<T> cmk(T r, T i) { return cx<T>{r, i}; }
+template <class T> TCYM_HD cx<T> operator+(cx<T> a, cx<T> b) { return {a.re + b.re, a.im + b.im}; }
+template <class T> TCYM_HD cx<T> operator-(cx<T> a, cx<T> b) { return {a.re - b.re, a.im - b.im}; }
+template <class T> TCYM_HD cx<T> operator*(cx<T> a, cx<T> b) { return {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re}; }
+template <class T> TCYM_HD cx<T> operator*(T s, cx<T> a) { return {s * a.re, s * a.im}; }
+template <class T> TCYM_HD cx<T> conj(cx<T> a) { return {a.re, -a.im}; }
+// acc + a*b, acc + a*conj(b), acc + conj(a)*conj(b)
+template <class T> TCYM_HD cx<T> cfma(cx<T> a, cx<T> b, cx<T> acc) {
+    return {fma(a.re, b.re, fma(-a.im, b.im, acc.re)), fma(a.re, b.im, fma(a.im, b.re, acc.im))};
+}
+template <class T> TCYM_HD cx<T> cfma_nc(cx<T> a, cx<T> b, cx<T> acc) {  // a * conj(b)
+    return {fma(a.re, b.re, fma(a.im, b.im, acc.re)), fma(a.im, b.re, fma(-a.re, b.im, acc.im))};
+}
+template <class T> TCYM_HD cx<T> cfma_cc(cx<T> a, cx<T> b, cx<T> acc) {  // conj(a) * conj(b)
+    return {fma(a.re, b.re, fma(-a.im, b.im, acc.re)), fma(-a.re, b.im, fma(-a.im, b.re, acc.im))};
+}
+template <class T> TCYM_HD cx<T> cfma_cn(cx<T> a, cx<T> b, cx<T> acc) {  // conj(a) * b
+    return {fma(a.re, b.re, fma(a.im, b.im, acc.re)), fma(a.re, b.im, fma(-a.im, b.re, acc.im))};
+}
+
+// ------------------------------------------------------------------ SU(2)
+template <class T> struct Q4 {
+    T q[4];  // q0,q1,q2: coefficients of i sigma_k; q3: identity
+};
+
+template <class T> struct SU2 {
+    using real = T;
+    using Mat = Q4<T>;
+    static constexpr int NA = 3;
+
+    static TCYM_HD Mat identity() { return Mat{{T(0), T(0), T(0), T(1)}}; }
+    static TCYM_HD Mat zero() { return Mat{{T(0), T(0), T(0), T(0)}}; }
+    static TCYM_HD Mat dag(const Mat &u) { return Mat{{-u.q[0], -u.q[1], -u.q[2], u.q[3]}}; }
+    static TCYM_HD Mat add(const Mat &a, const Mat &b) {
+        return Mat{{a.q[0] + b.q[0], a.q[1] + b.q[1], a.q[2] + b.q[2], a.q[3] + b.q[3]}};
+    }
+    static TCYM_HD Mat scale(T s, const Mat &a) { return Mat{{s * a.q[0], s * a.q[1], s * a.q[2], s * a.q[3]}}; }
+    // quaternion product (u3 + i u.s)(v3 + i v.s) = u3 v3 - u.v + i (u3 v + v3 u - u x v).s
+    // with optional conjugation of either factor
+    template <bool DA, bool DB> static TCYM_HD Mat mulx(const Mat &a, const Mat &b) {
+        const T sa = DA ? T(-1) : T(1), sb = DB ? T(-1) : T(1);
+        T u0 = sa * a.q[0], u1 = sa * a.q[1], u2 = sa * a.q[2], u3 = a.q[3];
+        T v0 = sb * b.q[0], v1 = sb * b.q[1], v2 = sb * b.q[2], v3 = b.q[3];
+        Mat w;
+        w.q[0] = fma(u3, v0, fma(v3, u0, -(u1 * v2 - u2 * v1)));
+        w.q[1] = fma(u3, v1, fma(v3, u1, -(u2 * v0 - u0 * v2)));
+        w.q[2] = fma(u3, v2, fma(v3, u2, -(u0 * v1 - u1 * v0)));
+        w.q[3] = fma(u3, v3, -fma(u0, v0, fma(u1, v1, u2 * v2)));
+        return w;
+    }
+    static TCYM_HD Mat mul(const Mat &a, const Mat &b) { return mulx<false, false>(a, b); }
+    // proj(u * a) for the force: Re tr(i t^k (u a)) = -(u a)_k
+    static TCYM_HD void proj_mul(const Mat &u, const Mat &a, T *out) {
+        Mat w = mulx<false, false>(u, a);
+        out[0] = -w.q[0]; out[1] = -w.q[1]; out[2] = -w.q[2];
+    }
+    static TCYM_HD void proj(const Mat &v, T *out) { out[0] = -v.q[0]; out[1] = -v.q[1]; out[2] = -v.q[2]; }
+    static TCYM_HD T retr_one_minus(const Mat &v) { return T(2) * (T(1) - v.q[3]); }
+    // exp(i c t^k e^k) = cos(d/2) + i sin(d/2) (c e / d).sigma, d = |c e|
+    static TCYM_HD Mat iexp(T c, const T *e) {
+        T x0 = c * e[0], x1 = c * e[1], x2 = c * e[2];
+        T d2 = fma(x0, x0, fma(x1, x1, x2 * x2));
+        if (d2 == T(0)) return identity();
+        T d = Real<T>::sqrt_(d2);
+        T s, co;
+        Real<T>::sincos_(T(0.5) * d, &s, &co);
+        T f = s / d;
+        return Mat{{f * x0, f * x1, f * x2, co}};
+    }
+    // components of V (e^k t^k) V^dagger: the pure quaternion (e,0) rotated
+    static TCYM_HD void adjoint(const Mat &v, const T *e, T *out) {
+        Mat q{{e[0], e[1], e[2], T(0)}};
+        Mat w = mulx<false, true>(mulx<false, false>(v, q), v);
+        out[0] = w.q[0]; out[1] = w.q[1]; out[2] = w.q[2];
+    }
+    static TCYM_HD void inverse_adjoint(const Mat &v, const T *e, T *out) {
+        Mat q{{e[0], e[1], e[2], T(0)}};
+        Mat w = mulx<false, false>(mulx<true, false>(v, q), v);
+        out[0] = w.q[0]; out[1] = w.q[1]; out[2] = w.q[2];
+    }
+    // ||V V^dagger - 1|| over the four components (SU2/GroupOperations.cpp:172-184)
+    static TCYM_HD T unitarity_norm(const Mat &v) {
+        Mat c = mulx<false, true>(v, v);
+        return Real<T>::sqrt_(c.q[0] * c.q[0] + c.q[1] * c.q[1] + c.q[2] * c.q[2] + (c.q[3] - T(1)) * (c.q[3] - T(1)));
+    }
+    static TCYM_HD Mat reunitarize(const Mat &v) {
+        T n = Real<T>::rsqrt_(v.q[0] * v.q[0] + v.q[1] * v.q[1] + v.q[2] * v.q[2] + v.q[3] * v.q[3]);
+        return scale(n, v);
+    }
+};
+
+// ------------------------------------------------------------------ SU(3)
+template <class T> struct M3 {
+    cx<T> m[3][3];  // row-major m[i][j]
+};
+
+template <class T> struct SU3 {
+    using real = T;
+    using Mat = M3<T>;
+    static constexpr int NA = 8;
+
+    static TCYM_HD Mat identity() {
+        Mat r;
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) r.m[i][j] = cx<T>{i == j ? T(1) : T(0), T(0)};
+        return r;
+    }
+    static TCYM_HD Mat zero() {
+        Mat r;
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) r.m[i][j] = cx<T>{T(0), T(0)};
+        return r;
+    }
+    static TCYM_HD Mat dag(const Mat &a) {
+        Mat r;
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) r.m[i][j] = conj(a.m[j][i]);
+        return r;
+    }
+    static TCYM_HD Mat add(const Mat &a, const Mat &b) {
+        Mat r;
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) r.m[i][j] = a.m[i][j] + b.m[i][j];
+        return r;
+    }
+    static TCYM_HD Mat scale(T s, const Mat &a) {
+        Mat r;
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) r.m[i][j] = s * a.m[i][j];
+        return r;
+    }
+    // a^(dagger if DA) * b^(dagger if DB)
+    template <bool DA, bool DB> static TCYM_HD Mat mulx(const Mat &a, const Mat &b) {
+        Mat r;
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                cx<T> acc{T(0), T(0)};
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    cx<T> x = DA ? a.m[k][i] : a.m[i][k];
+                    cx<T> y = DB ? b.m[j][k] : b.m[k][j];
+                    if (!DA && !DB) acc = cfma(x, y, acc);
+                    else if (!DA && DB) acc = cfma_nc(x, y, acc);
+                    else if (DA && !DB) acc = cfma_cn(x, y, acc);
+                    else acc = cfma_cc(x, y, acc);
+                }
+                r.m[i][j] = acc;
+            }
+        return r;
+    }
+    static TCYM_HD Mat mul(const Mat &a, const Mat &b) { return mulx<false, false>(a, b); }
+
+    // Re tr(i t^a V) for all a, V given by its entries; needs Im of the diagonal and
+    // both triangles off the diagonal (SU3/GroupOperations.cpp:108-118 expressions).
+    static TCYM_HD void proj(const Mat &v, T *p) {
+        const T is3 = T(0.57735026918962576450914878050196);
+        p[0] = T(-0.5) * (v.m[0][1].im + v.m[1][0].im);
+        p[1] = T(-0.5) * (v.m[0][1].re - v.m[1][0].re);
+        p[2] = T(-0.5) * (v.m[0][0].im - v.m[1][1].im);
+        p[3] = T(-0.5) * (v.m[0][2].im + v.m[2][0].im);
+        p[4] = T(-0.5) * (v.m[0][2].re - v.m[2][0].re);
+        p[5] = T(-0.5) * (v.m[1][2].im + v.m[2][1].im);
+        p[6] = T(-0.5) * (v.m[1][2].re - v.m[2][1].re);
+        p[7] = T(-0.5) * is3 * (v.m[0][0].im + v.m[1][1].im - T(2) * v.m[2][2].im);
+    }
+    // proj(u * a) computing only the entries proj reads: the six off-diagonal
+    // entries in full and the imaginary part of the diagonal.
+    static TCYM_HD void proj_mul(const Mat &u, const Mat &a, T *p) {
+        Mat w;
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                if (i == j) {
+                    T im = T(0);
+#pragma unroll
+                    for (int k = 0; k < 3; ++k) im = fma(u.m[i][k].re, a.m[k][j].im, fma(u.m[i][k].im, a.m[k][j].re, im));
+                    w.m[i][j] = cx<T>{T(0), im};
+                } else {
+                    cx<T> acc{T(0), T(0)};
+#pragma unroll
+                    for (int k = 0; k < 3; ++k) acc = cfma(u.m[i][k], a.m[k][j], acc);
+                    w.m[i][j] = acc;
+                }
+            }
+        proj(w, p);
+    }
+    static TCYM_HD T retr_one_minus(const Mat &v) { return T(3) - (v.m[0][0].re + v.m[1][1].re + v.m[2][2].re); }
+
+    // Hermitian H = e^a t^a
+    static TCYM_HD Mat algebra_matrix(T c, const T *e) {
+        const T is3 = T(0.57735026918962576450914878050196);
+        const T h = T(0.5) * c;
+        Mat q;
+        q.m[0][0] = cx<T>{h * (e[2] + e[7] * is3), T(0)};
+        q.m[1][1] = cx<T>{h * (-e[2] + e[7] * is3), T(0)};
+        q.m[2][2] = cx<T>{-c * e[7] * is3, T(0)};
+        q.m[1][0] = cx<T>{h * e[0], h * e[1]};
+        q.m[0][1] = cx<T>{h * e[0], -h * e[1]};
+        q.m[2][0] = cx<T>{h * e[3], h * e[4]};
+        q.m[0][2] = cx<T>{h * e[3], -h * e[4]};
+        q.m[2][1] = cx<T>{h * e[5], h * e[6]};
+        q.m[1][2] = cx<T>{h * e[5], -h * e[6]};
+        return q;
+    }
+    // x^a = 2 tr(t^a H) for Hermitian H
+    static TCYM_HD void algebra_components(const Mat &hm, T *x) {
+        const T is3 = T(0.57735026918962576450914878050196);
+        x[0] = hm.m[1][0].re + hm.m[0][1].re;
+        x[1] = hm.m[1][0].im - hm.m[0][1].im;
+        x[2] = hm.m[0][0].re - hm.m[1][1].re;
+        x[3] = hm.m[2][0].re + hm.m[0][2].re;
+        x[4] = hm.m[2][0].im - hm.m[0][2].im;
+        x[5] = hm.m[2][1].re + hm.m[1][2].re;
+        x[6] = hm.m[2][1].im - hm.m[1][2].im;
+        x[7] = is3 * (hm.m[0][0].re + hm.m[1][1].re - T(2) * hm.m[2][2].re);
+    }
+
+    // exp(i Q) for traceless Hermitian Q, see the file comment.
+    static TCYM_HD Mat iexp_hermitian(Mat q) {
+        // Q^2 (Hermitian): compute the upper triangle and mirror
+        Mat q2;
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = i; j < 3; ++j) {
+                cx<T> acc{T(0), T(0)};
+#pragma unroll
+                for (int k = 0; k < 3; ++k) acc = cfma(q.m[i][k], q.m[k][j], acc);
+                q2.m[i][j] = acc;
+                if (j != i) q2.m[j][i] = conj(acc);
+            }
+        T c1 = T(0.5) * (q2.m[0][0].re + q2.m[1][1].re + q2.m[2][2].re);
+        // spectral radius bound r^2 <= 4 c1 / 3; halve Q until r <= 1/2
+        int k = 0;
+        T r2 = c1 * T(4.0 / 3.0);
+        while (r2 > T(0.25) && k < 40) { r2 *= T(0.25); ++k; }
+        T s = T(1);
+        if (k > 0) {
+            s = T(1) / T(1ull << (k < 62 ? k : 62));
+            q = scale(s, q);
+            q2 = scale(s * s, q2);
+            c1 *= s * s;
+        }
+        // c0 = det Q (real for Hermitian Q)
+        cx<T> d = q.m[0][0] * (q.m[1][1] * q.m[2][2] - q.m[1][2] * q.m[2][1]) -
+                  q.m[0][1] * (q.m[1][0] * q.m[2][2] - q.m[1][2] * q.m[2][0]) +
+                  q.m[0][2] * (q.m[1][0] * q.m[2][1] - q.m[1][1] * q.m[2][0]);
+        T c0 = d.re;
+        // sum_n (i^n / n!) Q^n with Q^n = a_n + b_n Q + d_n Q^2
+        const int N = sizeof(T) == 4 ? 9 : 16;
+        T a = T(1), b = T(0), dd = T(0);
+        T f0r = T(1), f0i = T(0), f1r = T(0), f1i = T(0), f2r = T(0), f2i = T(0);
+        T fact = T(1);
+#pragma unroll
+        for (int n = 1; n <= N; ++n) {
+            T na = dd * c0, nb = fma(dd, c1, a), nd = b;
+            a = na; b = nb; dd = nd;
+            fact /= T(n);
+            T wa = fact * a, wb = fact * b, wd = fact * dd;
+            switch (n & 3) {  // i^n = 1, i, -1, -i
+                case 0: f0r += wa; f1r += wb; f2r += wd; break;
+                case 1: f0i += wa; f1i += wb; f2i += wd; break;
+                case 2: f0r -= wa; f1r -= wb; f2r -= wd; break;
+                default: f0i -= wa; f1i -= wb; f2i -= wd; break;
+            }
+        }
+        Mat r;
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                cx<T> x = q.m[i][j], y = q2.m[i][j];
+                T re = fma(f1r, x.re, fma(-f1i, x.im, fma(f2r, y.re, -f2i * y.im)));
+                T im = fma(f1r, x.im, fma(f1i, x.re, fma(f2r, y.im, f2i * y.re)));
+                if (i == j) { re += f0r; im += f0i; }
+                r.m[i][j] = cx<T>{re, im};
+            }
+        for (int it = 0; it < k; ++it) r = mul(r, r);
+        return r;
+    }
+    static TCYM_HD Mat iexp(T c, const T *e) { return iexp_hermitian(algebra_matrix(c, e)); }
+
+    // V (e^a t^a) V^dagger and V^dagger (e^a t^a) V in components
+    static TCYM_HD void adjoint(const Mat &v, const T *e, T *out) {
+        Mat h = algebra_matrix(T(1), e);
+        Mat w = mulx<false, true>(mulx<false, false>(v, h), v);
+        algebra_components(w, out);
+    }
+    static TCYM_HD void inverse_adjoint(const Mat &v, const T *e, T *out) {
+        Mat h = algebra_matrix(T(1), e);
+        Mat w = mulx<false, false>(mulx<true, false>(v, h), v);
+        algebra_components(w, out);
+    }
+    // ||V V^dagger - 1||_F (SU3/GroupOperations.cpp:351-363)
+    static TCYM_HD T unitarity_norm(const Mat &v) {
+        Mat c = mulx<false, true>(v, v);
+        T n = T(0);
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) {
+                T re = c.m[i][j].re - (i == j ? T(1) : T(0)), im = c.m[i][j].im;
+                n = fma(re, re, fma(im, im, n));
+            }
+        return Real<T>::sqrt_(n);
+    }
+    // third row of an SU(3) matrix from the first two: r2 = conj(r0 x r1)
+    static TCYM_HD void complete_row2(Mat &u) {
+        const cx<T> *a = u.m[0], *b = u.m[1];
+        u.m[2][0] = conj(a[1] * b[2] - a[2] * b[1]);
+        u.m[2][1] = conj(a[2] * b[0] - a[0] * b[2]);
+        u.m[2][2] = conj(a[0] * b[1] - a[1] * b[0]);
+    }
+    // Gram-Schmidt of rows 0 and 1, row 2 rebuilt: the nearest SU(3) matrix
+    // for a link that has drifted by rounding (not a max-trace projection).
+    static TCYM_HD Mat reunitarize(Mat u) {
+        T n0 = T(0);
+        for (int j = 0; j < 3; ++j) n0 = fma(u.m[0][j].re, u.m[0][j].re, fma(u.m[0][j].im, u.m[0][j].im, n0));
+        T i0 = Real<T>::rsqrt_(n0);
+        for (int j = 0; j < 3; ++j) u.m[0][j] = i0 * u.m[0][j];
+        cx<T> dot{T(0), T(0)};  // <r0, r1> = sum conj(r0) r1
+        for (int j = 0; j < 3; ++j) dot = cfma_cn(u.m[0][j], u.m[1][j], dot);
+        for (int j = 0; j < 3; ++j) u.m[1][j] = u.m[1][j] - dot * u.m[0][j];
+        T n1 = T(0);
+        for (int j = 0; j < 3; ++j) n1 = fma(u.m[1][j].re, u.m[1][j].re, fma(u.m[1][j].im, u.m[1][j].im, n1));
+        T i1 = Real<T>::rsqrt_(n1);
+        for (int j = 0; j < 3; ++j) u.m[1][j] = i1 * u.m[1][j];
+        complete_row2(u);
+        return u;
+    }
+};
+
+}  // namespace tcym

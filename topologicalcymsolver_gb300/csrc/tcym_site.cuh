@@ -1,0 +1,393 @@
+// Per-site work of every kernel, as __host__ __device__ functions of one site.
+//
+// A CUDA kernel maps one thread to one site and calls these; the test-only
+// host build calls them in a loop over sites, so CPU tests see the exact
+// arithmetic of the device path.
+#pragma once
+
+#include <type_traits>
+
+#include "tcym_layout.cuh"
+#include "tcym_rng.cuh"
+
+namespace tcym {
+
+// Step kinds: how the colour force f enters E before the link update.
+enum StepMode : int {
+    MODE_LEAPFROG = 0,  // E += fc f                              (Dynamics.cpp:184-188)
+    MODE_LANGEVIN = 1,  // E += fc f - damp E + kick xi           (LangevinDynamics.cpp:222-234)
+    MODE_FLOW = 2,      // E  = fc f  (the flow force, stored)    (GradientFlow.cpp:77-84)
+};
+
+// Coefficients of one step, per direction mu (metric factors of the reference
+// folded in; for unit spacings: fc = -2 dt (leapfrog/Langevin) or -2 (flow),
+// cnu = 1, uc = -dt or -dtau, damp = gamma dt, kick = sqrt(gamma dt) sqrt(2T)).
+template <class T> struct StepCoef {
+    int mode;
+    T fc[3], cnu[3], uc[3], damp[3], kick[3];
+    uint64_t seed, step;
+};
+
+// Staple sum around U_mu(x): A = sum_{nu != mu} cnu[nu] (S+ + S-) with
+//   S+ = U_nu(x+mu) U_mu^dag(x+nu) U_nu^dag(x)        (upper staple)
+//   S- = U_nu^dag(x+mu-nu) U_mu^dag(x-nu) U_nu(x-nu)  (lower staple)
+// so that U_mu(x) S+ is the plaquette U_{mu nu}(x) of Plaquettes.cpp:28 and
+// proj(U_mu S-) = -proj(U_{mu,-nu}(x)) (Plaquettes.cpp:30); the reference's
+// bracket [c_nu1 (P_{mu nu1} - P_{mu,-nu1}) - c_nu2 (P_{nu2 mu} - P_{-nu2,mu})]
+// (Dynamics.cpp:184-188) equals proj(U_mu A).
+template <class F>
+TCYM_HD typename F::Mat staple_sum(const void *U, int64_t V, const Nbhd &nb, int mu, const typename F::T *cnu) {
+    using G = typename F::G;
+    using M = typename F::Mat;
+    int dm[3];
+    unit(mu, dm);
+    M A = G::zero();
+#pragma unroll
+    for (int k = 1; k <= 2; ++k) {
+        const int nu = (mu + k) % 3;
+        int dn[3];
+        unit(nu, dn);
+        const int pm[3] = {dm[0] - dn[0], dm[1] - dn[1], dm[2] - dn[2]};
+        const int mn[3] = {-dn[0], -dn[1], -dn[2]};
+        M a1 = F::load(U, V, nu, nb.off(dm));
+        M a2 = F::load(U, V, mu, nb.off(dn));
+        M a3 = F::load(U, V, nu, nb.at(0, 0, 0));
+        M up = G::template mulx<false, true>(G::template mulx<false, true>(a1, a2), a3);
+        M b1 = F::load(U, V, nu, nb.off(pm));
+        M b2 = F::load(U, V, mu, nb.off(mn));
+        M b3 = F::load(U, V, nu, nb.off(mn));
+        M lo = G::template mulx<false, false>(G::template mulx<true, true>(b1, b2), b3);
+        A = G::add(A, G::scale(cnu[nu], G::add(up, lo)));
+    }
+    return A;
+}
+
+// One site of a step.  DO_E: compute the force and update E; DO_U: move the
+// links by exp(i uc E) and write them to Uout (Uout may alias Uin only when
+// DO_E is false, i.e. for the pointwise link update).
+template <class F, bool DO_E, bool DO_U>
+TCYM_HD void site_step(const Geom &g, const void *Uin, void *Uout, void *E, const StepCoef<typename F::T> &c,
+                       int64_t s) {
+    using G = typename F::G;
+    using T = typename F::T;
+    using M = typename F::Mat;
+    constexpr int NA = F::NA;
+    const int64_t V = g.V;
+    Nbhd nb(g, s);
+#pragma unroll 1
+    for (int mu = 0; mu < 3; ++mu) {
+        T e[NA];
+        F::load_e(E, V, mu, s, e);
+        M u = F::load(Uin, V, mu, s);
+        if (DO_E) {
+            M A = staple_sum<F>(Uin, V, nb, mu, c.cnu);
+            T f[NA];
+            G::proj_mul(u, A, f);
+            if (c.mode == MODE_LANGEVIN) {
+                T xi[NA];
+                normals<T, NA>(c.seed, STREAM_NOISE, c.step, (uint32_t)s, (uint32_t)mu, xi);
+#pragma unroll
+                for (int a = 0; a < NA; ++a) e[a] = e[a] + (c.fc[mu] * f[a] - c.damp[mu] * e[a] + c.kick[mu] * xi[a]);
+            } else if (c.mode == MODE_FLOW) {
+#pragma unroll
+                for (int a = 0; a < NA; ++a) e[a] = c.fc[mu] * f[a];
+            } else {
+#pragma unroll
+                for (int a = 0; a < NA; ++a) e[a] = e[a] + c.fc[mu] * f[a];
+            }
+            F::store_e(E, V, mu, s, e);
+        }
+        if (DO_U) {
+            M w = G::iexp(c.uc[mu], e);
+            F::store(Uout, V, mu, s, G::mul(w, u));
+        }
+    }
+}
+
+// Checkerboard flow: one link U_mu(x) of the active parity moved in place by
+// exp(-i dtau F_mu(x)), F = fc proj(U_mu A) (no reference counterpart; the
+// reference flows all links at once, GradientFlow.cpp:150-165).
+template <class F>
+TCYM_HD void link_flow(const Geom &g, void *U, int mu, const typename F::T *fc, const typename F::T *cnu,
+                       const typename F::T *uc, int64_t s) {
+    using G = typename F::G;
+    using T = typename F::T;
+    using M = typename F::Mat;
+    Nbhd nb(g, s);
+    M A = staple_sum<F>(U, g.V, nb, mu, cnu);
+    M u = F::load(U, g.V, mu, s);
+    T f[F::NA];
+    G::proj_mul(u, A, f);
+#pragma unroll
+    for (int a = 0; a < F::NA; ++a) f[a] *= fc[mu];
+    M w = G::iexp(uc[mu], f);
+    F::store(U, g.V, mu, s, G::mul(w, u));
+}
+
+// ----------------------------------------------------------------- observables
+// Plaquette P_{mu nu}(x) in the four quadrants around x, each a loop from x
+// (Plaquettes.cpp:28-31):
+//   Q0 = U_{mu nu}(x), Q1 = U_{-mu nu}(x), Q2 = U_{mu -nu}(x), Q3 = U_{-mu -nu}(x)
+template <class F>
+TCYM_HD void clover_leaves(const void *U, int64_t V, const Nbhd &nb, int mu, int nu, typename F::Mat *Q) {
+    using G = typename F::G;
+    using M = typename F::Mat;
+    int dm[3], dn[3];
+    unit(mu, dm);
+    unit(nu, dn);
+    const int o[3] = {0, 0, 0};
+    auto L = [&](int d, int x, int y, int z) { int t[3] = {x, y, z}; return F::load(U, V, d, nb.off(t)); };
+    // Q0 = U_mu(x) U_nu(x+mu) U_mu^dag(x+nu) U_nu^dag(x)
+    M a = L(mu, o[0], o[1], o[2]), b = L(nu, dm[0], dm[1], dm[2]), c = L(mu, dn[0], dn[1], dn[2]), d = L(nu, 0, 0, 0);
+    Q[0] = G::mul(G::mul(a, b), G::template mulx<true, true>(c, d));
+    // Q1 = U_nu(x) U_mu^dag(x+nu-mu) U_nu^dag(x-mu) U_mu(x-mu)
+    a = L(nu, 0, 0, 0);
+    b = L(mu, dn[0] - dm[0], dn[1] - dm[1], dn[2] - dm[2]);
+    c = L(nu, -dm[0], -dm[1], -dm[2]);
+    d = L(mu, -dm[0], -dm[1], -dm[2]);
+    Q[1] = G::mul(G::template mulx<false, true>(a, b), G::template mulx<true, false>(c, d));
+    // Q2 = U_nu^dag(x-nu) U_mu(x-nu) U_nu(x-nu+mu) U_mu^dag(x)
+    a = L(nu, -dn[0], -dn[1], -dn[2]);
+    b = L(mu, -dn[0], -dn[1], -dn[2]);
+    c = L(nu, dm[0] - dn[0], dm[1] - dn[1], dm[2] - dn[2]);
+    d = L(mu, 0, 0, 0);
+    Q[2] = G::mul(G::template mulx<true, false>(a, b), G::template mulx<false, true>(c, d));
+    // Q3 = U_mu^dag(x-mu) U_nu^dag(x-mu-nu) U_mu(x-mu-nu) U_nu(x-nu)
+    a = L(mu, -dm[0], -dm[1], -dm[2]);
+    b = L(nu, -dm[0] - dn[0], -dm[1] - dn[1], -dm[2] - dn[2]);
+    c = L(mu, -dm[0] - dn[0], -dm[1] - dn[1], -dm[2] - dn[2]);
+    d = L(nu, -dn[0], -dn[1], -dn[2]);
+    Q[3] = G::mul(G::template mulx<true, true>(a, b), G::mul(c, d));
+}
+
+// Everything the observables reduce, for one site (FP64 accumulators):
+//   esq[mu]   sum_a E^a_mu(x)^2                        (BulkObservables.cpp:99-130)
+//   bsq[i]    4 Re tr(1 - P_jk(x)), (i,j,k) cyclic      (BulkObservables.cpp:55-88)
+//   g[a]      Gauss violation G^a(x)                    (CALC/GaussViolation.cpp:13-23)
+//   un[mu]    ||U_mu U_mu^dag - 1||                     (UnitarityViolation.cpp:13-51)
+//   edotb     sum_i E_i^clover . B_i^clover             (ChernSimonsOperators.cpp:4-47)
+enum ObsMask : int { OBS_BULK = 1, OBS_GAUSS = 2, OBS_UNIT = 4, OBS_EDOTB = 8, OBS_ALL = 15 };
+
+template <class F> struct SiteObs {
+    double esq[3], bsq[3], g[F::NA], un[3], edotb;
+};
+
+template <class F>
+TCYM_HD void site_observables(const Geom &g, const void *U, const void *E, int mask, int64_t s, SiteObs<F> &o) {
+    using G = typename F::G;
+    using T = typename F::T;
+    using M = typename F::Mat;
+    constexpr int NA = F::NA;
+    const int64_t V = g.V;
+    Nbhd nb(g, s);
+    for (int mu = 0; mu < 3; ++mu) { o.esq[mu] = 0; o.bsq[mu] = 0; o.un[mu] = 0; }
+    for (int a = 0; a < NA; ++a) o.g[a] = 0;
+    o.edotb = 0;
+    T et[3][NA];  // U_mu^dag(x-mu) E_mu(x-mu) U_mu(x-mu): shared by Gauss and clover E
+    if (mask & (OBS_GAUSS | OBS_EDOTB)) {
+        for (int mu = 0; mu < 3; ++mu) {
+            int d[3];
+            unit(mu, d);
+            const int m[3] = {-d[0], -d[1], -d[2]};
+            int64_t sm = nb.off(m);
+            T e[NA];
+            F::load_e(E, V, mu, sm, e);
+            G::inverse_adjoint(F::load(U, V, mu, sm), e, et[mu]);
+        }
+    }
+    for (int mu = 0; mu < 3; ++mu) {
+        T e[NA];
+        F::load_e(E, V, mu, s, e);
+        double sq = 0;
+        for (int a = 0; a < NA; ++a) sq += (double)e[a] * (double)e[a];
+        o.esq[mu] = sq;
+        if (mask & OBS_GAUSS)
+            for (int a = 0; a < NA; ++a) o.g[a] += (double)e[a] - (double)et[mu][a];
+        if (mask & OBS_UNIT) o.un[mu] = (double)G::unitarity_norm(F::load(U, V, mu, s));
+        if (mask & (OBS_BULK | OBS_EDOTB)) {
+            // plane (j,k) = (mu+1, mu+2): B_mu
+            const int j = (mu + 1) % 3, k = (mu + 2) % 3;
+            M Q[4];
+            if (mask & OBS_EDOTB) {
+                clover_leaves<F>(U, V, nb, j, k, Q);
+            } else {
+                int dj[3], dk[3];
+                unit(j, dj);
+                unit(k, dk);
+                M a = F::load(U, V, j, s), b = F::load(U, V, k, nb.off(dj)), c = F::load(U, V, j, nb.off(dk)),
+                  d = F::load(U, V, k, s);
+                Q[0] = G::mul(G::mul(a, b), G::template mulx<true, true>(c, d));
+            }
+            o.bsq[mu] = 4.0 * (double)G::retr_one_minus(Q[0]);
+            if (mask & OBS_EDOTB) {
+                M avg = G::scale(T(0.25), G::add(G::add(Q[0], Q[1]), G::add(Q[2], Q[3])));
+                T b[NA];
+                G::proj(avg, b);
+                double dot = 0;
+                for (int a = 0; a < NA; ++a) dot += 0.5 * ((double)e[a] + (double)et[mu][a]) * 2.0 * (double)b[a];
+                o.edotb += dot;
+            }
+        }
+    }
+}
+
+// Gauss violation G(x) in working precision T, for the restore iteration.
+template <class F>
+TCYM_HD void site_gauss(const Geom &g, const void *U, const void *E, int64_t s, double *gv) {
+    using G = typename F::G;
+    using T = typename F::T;
+    constexpr int NA = F::NA;
+    Nbhd nb(g, s);
+    for (int a = 0; a < NA; ++a) gv[a] = 0;
+    for (int mu = 0; mu < 3; ++mu) {
+        int d[3];
+        unit(mu, d);
+        const int m[3] = {-d[0], -d[1], -d[2]};
+        int64_t sm = nb.off(m);
+        T e[NA], em[NA], t[NA];
+        F::load_e(E, g.V, mu, s, e);
+        F::load_e(E, g.V, mu, sm, em);
+        G::inverse_adjoint(F::load(U, g.V, mu, sm), em, t);
+        for (int a = 0; a < NA; ++a) gv[a] += (double)e[a] - (double)t[a];
+    }
+}
+
+// E_mu(x) -= gam (G(x) - U_mu(x) G(x+mu) U_mu^dag(x))   (GaussRestore.cpp:73-113)
+// G is an FP64 SoA scratch array G[a*V + site].
+template <class F>
+TCYM_HD void site_gauss_update(const Geom &g, const void *U, void *E, const double *Gs, double gam, int64_t s) {
+    using G = typename F::G;
+    using T = typename F::T;
+    constexpr int NA = F::NA;
+    Nbhd nb(g, s);
+    for (int mu = 0; mu < 3; ++mu) {
+        int d[3];
+        unit(mu, d);
+        int64_t sp = nb.off(d);
+        T gp[NA], t[NA], e[NA];
+        for (int a = 0; a < NA; ++a) gp[a] = (T)Gs[a * g.V + sp];
+        G::adjoint(F::load(U, g.V, mu, s), gp, t);
+        F::load_e(E, g.V, mu, s, e);
+        for (int a = 0; a < NA; ++a) e[a] = (T)((double)e[a] - gam * (Gs[a * g.V + s] - (double)t[a]));
+        F::store_e(E, g.V, mu, s, e);
+    }
+}
+
+// ------------------------------------------------------------ initial conditions
+template <class F> TCYM_HD void site_set_zero(const Geom &g, void *U, void *E, int64_t s) {
+    using T = typename F::T;
+    T z[F::NA];
+    for (int a = 0; a < F::NA; ++a) z[a] = T(0);
+    for (int mu = 0; mu < 3; ++mu) {
+        F::store(U, g.V, mu, s, F::G::identity());
+        F::store_e(E, g.V, mu, s, z);
+    }
+}
+
+// E^a_mu(x) = sigma N(0,1) (field stream); computed in FP64 and rounded.
+template <class F> TCYM_HD void site_gaussian_efield(const Geom &g, void *E, double sigma, uint64_t seed, int64_t s) {
+    using T = typename F::T;
+    for (int mu = 0; mu < 3; ++mu) {
+        double z[F::NA];
+        normals<double, F::NA>(seed, STREAM_EFIELD, 0, (uint32_t)s, (uint32_t)mu, z);
+        T e[F::NA];
+        for (int a = 0; a < F::NA; ++a) e[a] = (T)(sigma * z[a]);
+        F::store_e(E, g.V, mu, s, e);
+    }
+}
+
+// U_mu(x) = exp(i t^a theta^a), theta^a = sigma N(0,1) (link stream); FP64 then rounded.
+template <class F> TCYM_HD void site_random_links(const Geom &g, void *U, double sigma, uint64_t seed, int64_t s) {
+    using G64 = typename std::conditional<F::NA == 3, SU2<double>, SU3<double>>::type;
+    using T = typename F::T;
+    for (int mu = 0; mu < 3; ++mu) {
+        double th[F::NA];
+        normals<double, F::NA>(seed, STREAM_LINKS, 0, (uint32_t)s, (uint32_t)mu, th);
+        for (int a = 0; a < F::NA; ++a) th[a] *= sigma;
+        typename G64::Mat m = G64::iexp(1.0, th);
+        typename F::Mat r;
+        if constexpr (F::NA == 3) {
+            for (int k = 0; k < 4; ++k) r.q[k] = (T)m.q[k];
+        } else {
+            for (int i = 0; i < 3; ++i)
+                for (int j = 0; j < 3; ++j) r.m[i][j] = cx<T>{(T)m.m[i][j].re, (T)m.m[i][j].im};
+        }
+        F::store(U, g.V, mu, s, r);
+    }
+}
+
+// FP64 reunitarisation of the stored links (new: the reference only monitors
+// unitarity).  Links are widened to FP64, projected and rounded back.
+template <class F> TCYM_HD void site_reunitarize(const Geom &g, void *U, int64_t s) {
+    using G64 = typename std::conditional<F::NA == 3, SU2<double>, SU3<double>>::type;
+    using T = typename F::T;
+    for (int mu = 0; mu < 3; ++mu) {
+        typename F::Mat m = F::load(U, g.V, mu, s);
+        typename G64::Mat d;
+        if constexpr (F::NA == 3) {
+            for (int k = 0; k < 4; ++k) d.q[k] = (double)m.q[k];
+        } else {
+            for (int i = 0; i < 3; ++i)
+                for (int j = 0; j < 3; ++j) d.m[i][j] = cx<double>{(double)m.m[i][j].re, (double)m.m[i][j].im};
+        }
+        d = G64::reunitarize(d);
+        if constexpr (F::NA == 3) {
+            for (int k = 0; k < 4; ++k) m.q[k] = (T)d.q[k];
+        } else {
+            for (int i = 0; i < 3; ++i)
+                for (int j = 0; j < 3; ++j) m.m[i][j] = cx<T>{(T)d.m[i][j].re, (T)d.m[i][j].im};
+        }
+        F::store(U, g.V, mu, s, m);
+    }
+}
+
+// ----------------------------------------------------------- AoS conversion
+template <class F> TCYM_HD void site_from_aos(const Geom &g, void *U, void *E, const double *Ua, const double *Ea, int64_t s) {
+    using T = typename F::T;
+    constexpr int NMD = F::NA == 3 ? 4 : 18;
+    for (int mu = 0; mu < 3; ++mu) {
+        if (Ua) {
+            typename F::Mat m;
+            if constexpr (F::NA == 3) {
+                for (int k = 0; k < 4; ++k) m.q[k] = (T)Ua[NMD * (mu + 3 * s) + k];
+            } else {
+                const double *a = Ua + NMD * (mu + 3 * s);
+                for (int i = 0; i < 3; ++i)
+                    for (int j = 0; j < 3; ++j) m.m[i][j] = cx<T>{(T)a[2 * (i + 3 * j)], (T)a[2 * (i + 3 * j) + 1]};
+            }
+            F::store(U, g.V, mu, s, m);
+        }
+        if (Ea) {
+            T e[F::NA];
+            for (int a = 0; a < F::NA; ++a) e[a] = (T)Ea[F::NA * (mu + 3 * s) + a];
+            F::store_e(E, g.V, mu, s, e);
+        }
+    }
+}
+
+template <class F> TCYM_HD void site_to_aos(const Geom &g, const void *U, const void *E, double *Ua, double *Ea, int64_t s) {
+    using T = typename F::T;
+    constexpr int NMD = F::NA == 3 ? 4 : 18;
+    for (int mu = 0; mu < 3; ++mu) {
+        if (Ua) {
+            typename F::Mat m = F::load(U, g.V, mu, s);
+            if constexpr (F::NA == 3) {
+                for (int k = 0; k < 4; ++k) Ua[NMD * (mu + 3 * s) + k] = (double)m.q[k];
+            } else {
+                double *a = Ua + NMD * (mu + 3 * s);
+                for (int i = 0; i < 3; ++i)
+                    for (int j = 0; j < 3; ++j) {
+                        a[2 * (i + 3 * j)] = (double)m.m[i][j].re;
+                        a[2 * (i + 3 * j) + 1] = (double)m.m[i][j].im;
+                    }
+            }
+        }
+        if (Ea) {
+            T e[F::NA];
+            F::load_e(E, g.V, mu, s, e);
+            for (int a = 0; a < F::NA; ++a) Ea[F::NA * (mu + 3 * s) + a] = (double)e[a];
+        }
+    }
+}
+
+}  // namespace tcym
