@@ -110,6 +110,9 @@ int tcym_lattice_download(tcym_lattice lat, double *U_aos, double *E_aos);
 int tcym_lattice_copy(tcym_lattice dst, const tcym_lattice src);
 /* Waits for all work queued on the lattice. */
 int tcym_lattice_sync(tcym_lattice lat);
+/* The lattice's CUDA stream (a cudaStream_t), for ordering or timing caller work
+ * against the library's kernels. */
+int tcym_lattice_stream(tcym_lattice lat, void **stream);
 
 /* ------------------------------------------------------ initial conditions */
 /* InitialConditions::SetZero (INITIALCONDITIONS/SetZero.cpp:3-24): U = 1, E = 0. */

@@ -1,0 +1,116 @@
+"""Generate the golden fixtures of tests/golden/ from the reference's own code.
+
+Runs the reference's hot-path sources compiled in place (oracle/_ref, built by
+``make -C oracle ref`` from the reference tree) on small seeded inputs and
+stores inputs and outputs as .npz.  The reference tree is needed only to
+regenerate; the fixtures are committed and the tests read them anywhere.
+
+Inputs are built with the oracle's Philox generators (the same streams the
+CUDA library draws); every output below is produced by the reference itself:
+  ref_states_su{2,3}.npz   (4,5,6) lattice: leapfrog 1/10/100 steps (dt 0.05),
+                           Langevin 10 steps (dt 0.02, gamma 1, T 0.6, seed 3),
+                           gradient flow 10 steps (dtau 0.02, CalibrationUpdate),
+                           Gauss restore, and the observables of each state
+  ref_group_su{2,3}.npz    MatrixIExp, ReTrIGenU, (Inverse)AdjointMultiplication
+  ref_c0_su2_16.npz        BASELINE config 0: SU(2) 16^3, U = 1, E ~ N(0, 1/2)
+                           (seed 1) Gauss-restored by the reference, 1000 leapfrog
+                           steps at dt 0.05, observables every 10 steps
+
+  python tests/golden/make_golden.py
+"""
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+import oracle  # noqa: E402
+
+SHAPE = (4, 5, 6)
+
+
+def states(nc):
+    P, R = oracle.Port(nc), oracle.Ref(nc)
+    U0, E0 = oracle.empty_fields(nc, SHAPE)
+    P.random_links(SHAPE, U0, 0.6, 101 + nc)
+    P.gaussian_efield(SHAPE, E0, 0.7, 201 + nc)
+    R.init(SHAPE)
+    out = {"U0": U0, "E0": E0, "shape": np.array(SHAPE)}
+
+    def obs(tag):
+        out["obs_" + tag] = R.observables()
+
+    R.set(U0, E0)
+    obs("0")
+    R.leapfrog(0.05, 1)
+    out["U_lf1"], out["E_lf1"] = R.get()
+    obs("lf1")
+    R.leapfrog(0.05, 9)
+    out["U_lf10"], out["E_lf10"] = R.get()
+    obs("lf10")
+    R.leapfrog(0.05, 90)
+    out["U_lf100"], out["E_lf100"] = R.get()
+    obs("lf100")
+
+    R.set(U0, E0)
+    R.langevin(0.02, 0.6, 3, 0, 10)
+    out["U_lv10"], out["E_lv10"] = R.get()
+    obs("lv10")
+
+    R.set(U0, E0)
+    out["dncs_fl10"] = np.array(R.flow(np.sqrt(0.02), 10, 1))
+    out["U_fl10"], out["E_fl10"] = R.get()
+    obs("fl10")
+
+    R.set(U0, E0)
+    R.gauss_restore()
+    out["U_gr"], out["E_gr"] = R.get()
+    obs("gr")
+    np.savez_compressed(os.path.join(HERE, f"ref_states_su{nc}.npz"), **out)
+
+
+def group(nc):
+    R = oracle.Ref(nc)
+    rng = np.random.default_rng(7 + nc)
+    na = oracle.NA[nc]
+    n = 12
+    alpha = rng.normal(size=(n, na)) * np.repeat([1e-4, 0.1, 1.0, 4.0], 3)[:, None]
+    c = rng.normal(size=n)
+    exps = np.array([R.matrix_iexp(c[i], alpha[i]) for i in range(n)])
+    e = rng.normal(size=(n, na))
+    proj = np.array([R.retr_igen(exps[i] * 1.1) for i in range(n)])
+    adj = np.array([R.adjoint(exps[i], e[i]) for i in range(n)])
+    iadj = np.array([R.inverse_adjoint(exps[i], e[i]) for i in range(n)])
+    np.savez_compressed(os.path.join(HERE, f"ref_group_su{nc}.npz"), alpha=alpha, c=c, exp=exps, e=e, proj=proj,
+                        adj=adj, iadj=iadj)
+
+
+def config0():
+    R = oracle.Ref(2)
+    shape = (16, 16, 16)
+    R.init(shape)
+    R.set_zero()
+    R.thermal_efield(2.0, 1)  # E = N(0,1)/sqrt(2) then Restore (ThermalDynamics.cpp:205-226)
+    U, E = R.get()
+    series = [R.observables()]
+    for _ in range(100):
+        R.leapfrog(0.05, 10)
+        series.append(R.observables())
+    np.savez_compressed(os.path.join(HERE, "ref_c0_su2_16.npz"), E_ic=E, series=np.array(series), dt=0.05,
+                        every=10)
+
+
+if __name__ == "__main__":
+    oracle.build()
+    if not (oracle.ref_available(2) and oracle.ref_available(3)):
+        sys.exit("the reference's sources must be compiled first: make -C oracle ref")
+    for nc in (2, 3):
+        states(nc)
+        group(nc)
+    config0()
+    for f in sorted(os.listdir(HERE)):
+        if f.endswith(".npz"):
+            print(f, os.path.getsize(os.path.join(HERE, f)))

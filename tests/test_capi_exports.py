@@ -1,0 +1,53 @@
+"""The C-ABI library loads without a GPU and exports every function declared in include/*.h."""
+import ctypes
+import os
+import re
+
+import pytest
+
+from topologicalcymsolver_gb300 import build
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    names = set()
+    inc = os.path.join(ROOT, "include")
+    for f in os.listdir(inc):
+        if not f.endswith(".h"):
+            continue
+        src = open(os.path.join(inc, f)).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        for m in re.finditer(r"^\s*(?:const\s+)?[A-Za-z_][\w\s\*]*?\b(tcym_\w+)\s*\(", src, flags=re.M):
+            names.add(m.group(1))
+    return sorted(names)
+
+
+def test_header_declares_entry_points():
+    names = declared_functions()
+    assert "tcym_leapfrog" in names and "tcym_observables" in names and len(names) > 25
+
+
+def test_library_exports_every_declared_symbol():
+    lib = build.build_library()
+    L = ctypes.CDLL(lib)
+    missing = [n for n in declared_functions() if not hasattr(L, n)]
+    assert not missing, missing
+
+
+def test_version_without_gpu():
+    L = ctypes.CDLL(build.build_library())
+    assert L.tcym_version() == 100
+
+
+def test_context_fails_cleanly_without_gpu():
+    """On a host without a CUDA device the library reports an error code instead of aborting."""
+    try:
+        import torch
+        if torch.cuda.is_available():
+            pytest.skip("a GPU is present")
+    except ImportError:
+        pass
+    L = ctypes.CDLL(build.build_library())
+    h = ctypes.c_void_p()
+    assert L.tcym_ctx_create(0, ctypes.byref(h)) != 0

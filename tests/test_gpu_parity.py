@@ -1,0 +1,197 @@
+"""GPU parity: the sm_103a kernels through the C ABI against the FP64 oracle.
+
+Tolerances (spec contract): FP64 device path <= 1e-10 relative over short
+windows (<= 100 steps), FP32 storage path <= 1e-5 relative.  "Relative" is the
+max-abs difference over the max-abs magnitude of the oracle's array.
+"""
+import numpy as np
+import pytest
+
+import oracle
+import topologicalcymsolver_gb300 as tcym
+
+pytestmark = pytest.mark.gpu
+
+TOL = {tcym.FP64: 1e-10, tcym.FP32: 1e-5}
+PREC = [pytest.param(tcym.FP64, id="fp64"), pytest.param(tcym.FP32, id="fp32")]
+GROUPS = [pytest.param(2, id="su2"), pytest.param(3, id="su3")]
+
+
+def rel(a, b):
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+
+def random_state(P, nc, shape, seed=3, sigma_u=0.6, sigma_e=0.7):
+    U, E = oracle.empty_fields(nc, shape)
+    P.random_links(shape, U, sigma_u, seed)
+    P.gaussian_efield(shape, E, sigma_e, seed + 1)
+    return U, E
+
+
+@pytest.mark.parametrize("prec", PREC)
+@pytest.mark.parametrize("nc", GROUPS)
+@pytest.mark.parametrize("shape", [(6, 6, 6), (5, 6, 7)])
+def test_leapfrog_parity(ctx, oracle_port, nc, prec, shape):
+    P = oracle_port[nc]
+    U, E = random_state(P, nc, shape)
+    lat = tcym.Lattice(ctx, nc, shape, prec)
+    lat.set_reunitarize_period(0)
+    lat.upload(U, E)
+    for nsteps in (1, 9, 90):  # cumulative 1, 10, 100 steps at dt = 0.05
+        lat.leapfrog(0.05, nsteps)
+        P.leapfrog(shape, U, E, 0.05, nsteps)
+        Ug, Eg = lat.download()
+        assert rel(Ug, U) < TOL[prec], (nsteps, rel(Ug, U))
+        assert rel(Eg, E) < TOL[prec], (nsteps, rel(Eg, E))
+
+
+@pytest.mark.parametrize("prec", PREC)
+@pytest.mark.parametrize("nc", GROUPS)
+def test_split_updates_parity(ctx, oracle_port, nc, prec):
+    """Dynamics::UpdateElectricFields and UpdateGaugeLinks called separately."""
+    shape = (4, 6, 5)
+    P = oracle_port[nc]
+    U, E = random_state(P, nc, shape, seed=11)
+    lat = tcym.Lattice(ctx, nc, shape, prec)
+    lat.upload(U, E)
+    lat.update_e(0.03)
+    P.update_e(shape, U, E, 0.03)
+    Ug, Eg = lat.download()
+    assert rel(Eg, E) < TOL[prec]
+    lat.update_u(0.03)
+    P.update_u(shape, U, E, 0.03)
+    Ug, Eg = lat.download()
+    assert rel(Ug, U) < TOL[prec]
+
+
+@pytest.mark.parametrize("prec", PREC)
+@pytest.mark.parametrize("nc", GROUPS)
+def test_langevin_parity_same_noise(ctx, oracle_port, nc, prec):
+    shape = (6, 5, 6)
+    P = oracle_port[nc]
+    U, E = random_state(P, nc, shape, seed=21)
+    lat = tcym.Lattice(ctx, nc, shape, prec)
+    lat.set_reunitarize_period(0)
+    lat.upload(U, E)
+    lat.langevin(0.02, 1.0, 0.6, 3, 0, 20)
+    P.langevin(shape, U, E, 0.02, 1.0, 0.6, 3, 0, 20)
+    Ug, Eg = lat.download()
+    assert rel(Ug, U) < TOL[prec]
+    assert rel(Eg, E) < TOL[prec]
+
+
+@pytest.mark.parametrize("prec", PREC)
+@pytest.mark.parametrize("nc", GROUPS)
+def test_flow_parity(ctx, oracle_port, nc, prec):
+    shape = (6, 6, 4)
+    P = oracle_port[nc]
+    U, E = random_state(P, nc, shape, seed=31)
+    lat = tcym.Lattice(ctx, nc, shape, prec)
+    lat.upload(U, E)
+    d_gpu = lat.flow(0.02, 5, tcym.FLOW_SIMULTANEOUS, calibrate=True)
+    d_orc = P.flow(shape, U, E, 0.02, 5, 1)
+    Ug, Eg = lat.download()
+    assert rel(Ug, U) < TOL[prec]
+    assert rel(Eg, E) < TOL[prec]
+    assert abs(d_gpu - d_orc) < TOL[prec] * max(abs(d_orc), 1e-3) * 10
+    # checkerboard sweeps (in place, parity x direction order)
+    lat.flow(0.02, 3, tcym.FLOW_CHECKERBOARD)
+    P.flow_checkerboard(shape, U, 0.02, 3)
+    Ug, _ = lat.download()
+    assert rel(Ug, U) < TOL[prec]
+
+
+@pytest.mark.parametrize("prec", PREC)
+@pytest.mark.parametrize("nc", GROUPS)
+def test_observables_parity(ctx, oracle_port, nc, prec):
+    shape = (5, 6, 4)
+    P = oracle_port[nc]
+    U, E = random_state(P, nc, shape, seed=41)
+    lat = tcym.Lattice(ctx, nc, shape, prec)
+    lat.upload(U, E)
+    if prec == tcym.FP32:  # compare against the oracle on the rounded state
+        U, E = lat.download()
+    o = lat.observables().as_oracle_vector()
+    r = P.observables(shape, U, E)
+    tol = 1e-12 if prec == tcym.FP64 else 1e-5
+    for k in list(range(0, 11)) + [13, 15]:
+        assert abs(o[k] - r[k]) <= tol * max(1.0, abs(r[k])), (oracle.OBS_FIELDS[k], o[k], r[k])
+    # unitarity: FP32 links carry rounding at 1e-7
+    assert abs(o[11] - r[11]) <= (1e-12 if prec == tcym.FP64 else 1e-6)
+
+
+@pytest.mark.parametrize("nc", GROUPS)
+def test_initial_conditions_match_oracle(ctx, oracle_port, nc):
+    shape = (4, 5, 6)
+    P = oracle_port[nc]
+    U, E = oracle.empty_fields(nc, shape)
+    P.random_links(shape, U, 0.3, 2)
+    P.gaussian_efield(shape, E, np.sqrt(0.5), 1)
+    lat = tcym.Lattice(ctx, nc, shape, tcym.FP64)
+    lat.random_links(0.3, 2)
+    lat.gaussian_efield(np.sqrt(0.5), 1)
+    Ug, Eg = lat.download()
+    assert rel(Eg, E) < 1e-14
+    assert rel(Ug, U) < 1e-13
+    lat.set_zero()
+    P.set_zero(shape, U, E)
+    Ug, Eg = lat.download()
+    assert np.array_equal(Ug, U) and np.array_equal(Eg, E)
+
+
+@pytest.mark.parametrize("nc", GROUPS)
+def test_gauss_restore(ctx, oracle_port, nc):
+    shape = (6, 6, 6)
+    P = oracle_port[nc]
+    U, E = random_state(P, nc, shape, seed=51)
+    lat = tcym.Lattice(ctx, nc, shape, tcym.FP64)
+    lat.upload(U, E)
+    it_g, mx = lat.gauss_restore(1e-14, 10000)
+    it_o = P.gauss_restore(shape, U, E, 1e-14, 10000)
+    Ug, Eg = lat.download()
+    assert abs(it_g - it_o) <= 1  # the max crosses tol at the same iteration up to rounding
+    assert rel(Eg, E) < 1e-10
+    o = P.observables(shape, Ug, Eg)
+    assert o[9] <= 1e-13 and o[15] < 1e-12
+
+
+@pytest.mark.parametrize("nc", GROUPS)
+def test_upload_download_roundtrip(ctx, oracle_port, nc):
+    shape = (3, 4, 5)
+    P = oracle_port[nc]
+    U, E = random_state(P, nc, shape)
+    lat = tcym.Lattice(ctx, nc, shape, tcym.FP64)
+    lat.upload(U, E)
+    Ug, Eg = lat.download()
+    assert np.array_equal(Ug, U) and np.array_equal(Eg, E)
+    lat32 = tcym.Lattice(ctx, nc, shape, tcym.FP32)
+    lat32.upload(U, E)
+    Ug, Eg = lat32.download()
+    assert rel(Ug, U) < 2e-7 and rel(Eg, E) < 1e-7
+
+
+@pytest.mark.parametrize("nc", GROUPS)
+def test_ncs_tracking_is_kahan_sum_of_edotb(ctx, oracle_port, nc):
+    shape = (6, 6, 6)
+    P = oracle_port[nc]
+    U, E = random_state(P, nc, shape, seed=61)
+    lat = tcym.Lattice(ctx, nc, shape, tcym.FP64)
+    lat.upload(U, E)
+    lat.ncs_track(1)
+    lat.ncs_reset()
+    dt, total = 0.05, 0.0
+    for _ in range(10):
+        lat.leapfrog(dt, 1)
+        P.leapfrog(shape, U, E, dt, 1)
+        total += dt * P.edotb_clover(shape, U, E) / (8 * np.pi ** 2)
+    assert abs(lat.ncs() - total) < 1e-11 * max(1.0, abs(total))
+
+
+def test_error_codes(ctx):
+    with pytest.raises(tcym.TcymError) as ei:
+        tcym.Lattice(ctx, 4, (4, 4, 4))
+    assert ei.value.code == 1
+    lat = tcym.Lattice(ctx, 2, (5, 4, 4))
+    with pytest.raises(tcym.TcymError) as ei:
+        lat.flow(0.01, 1, tcym.FLOW_CHECKERBOARD)  # odd extent
+    assert ei.value.code == 1

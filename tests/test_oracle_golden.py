@@ -1,0 +1,123 @@
+"""The oracle (FP64 C restatement) pinned against the reference's own outputs.
+
+Fixtures under tests/golden/ were produced by the reference's sources compiled
+in place (tests/golden/make_golden.py).  The oracle must reproduce them to
+FP64 rounding: 1e-12 relative for single steps and observables; 1e-10 after
+100 leapfrog steps (the SU(3) exponential uses another eigensolver, so
+rounding differs at 1e-16 per step and grows slowly in the chaotic dynamics).
+"""
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+
+G = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def rel(a, b):
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+
+def load(name):
+    return dict(np.load(os.path.join(G, name)))
+
+
+@pytest.mark.parametrize("nc", [2, 3])
+def test_group_kats(oracle_port, nc):
+    P = oracle_port[nc]
+    d = load(f"ref_group_su{nc}.npz")
+    for i in range(len(d["c"])):
+        assert np.abs(P.matrix_iexp(d["c"][i], d["alpha"][i]) - d["exp"][i]).max() < 2e-14
+        assert np.abs(P.retr_igen(d["exp"][i] * 1.1) - d["proj"][i]).max() < 1e-15
+        assert np.abs(P.adjoint(d["exp"][i], d["e"][i]) - d["adj"][i]).max() < 1e-14
+        assert np.abs(P.inverse_adjoint(d["exp"][i], d["e"][i]) - d["iadj"][i]).max() < 1e-14
+
+
+@pytest.mark.parametrize("nc", [2, 3])
+def test_states_leapfrog(oracle_port, nc):
+    P = oracle_port[nc]
+    d = load(f"ref_states_su{nc}.npz")
+    shape = tuple(d["shape"])
+    U, E = d["U0"].copy(), d["E0"].copy()
+    for n, tag, tol in ((1, "lf1", 1e-13), (9, "lf10", 1e-12), (90, "lf100", 1e-10)):
+        P.leapfrog(shape, U, E, 0.05, n)
+        assert rel(U, d["U_" + tag]) < tol
+        assert rel(E, d["E_" + tag]) < tol
+        o = P.observables(shape, U, E)
+        r = d["obs_" + tag]
+        for k in range(14):
+            assert abs(o[k] - r[k]) < 1e-9 * max(1.0, abs(r[k])), (tag, oracle.OBS_FIELDS[k])
+
+
+@pytest.mark.parametrize("nc", [2, 3])
+def test_states_langevin_same_noise(oracle_port, nc):
+    P = oracle_port[nc]
+    d = load(f"ref_states_su{nc}.npz")
+    shape = tuple(d["shape"])
+    U, E = d["U0"].copy(), d["E0"].copy()
+    P.langevin(shape, U, E, 0.02, 1.0, 0.6, 3, 0, 10)
+    assert rel(U, d["U_lv10"]) < 1e-12
+    assert rel(E, d["E_lv10"]) < 1e-12
+
+
+@pytest.mark.parametrize("nc", [2, 3])
+def test_states_flow_and_calibration(oracle_port, nc):
+    P = oracle_port[nc]
+    d = load(f"ref_states_su{nc}.npz")
+    shape = tuple(d["shape"])
+    U, E = d["U0"].copy(), d["E0"].copy()
+    P.flow(shape, U, E, 0.02, 10, 0)
+    assert rel(U, d["U_fl10"]) < 1e-12
+    assert rel(E, d["E_fl10"]) < 1e-12
+    # the reference's calibration uses the O(a^2)-improved E.B: compare the state only,
+    # and the clover E.B of the flowed state through the observables
+    o = P.observables(shape, U, E)
+    assert abs(o[13] - d["obs_fl10"][13]) < 1e-10 * max(1.0, abs(d["obs_fl10"][13]))
+
+
+@pytest.mark.parametrize("nc", [2, 3])
+def test_states_gauss_restore(oracle_port, nc):
+    P = oracle_port[nc]
+    d = load(f"ref_states_su{nc}.npz")
+    shape = tuple(d["shape"])
+    U, E = d["U0"].copy(), d["E0"].copy()
+    P.gauss_restore(shape, U, E)
+    assert rel(E, d["E_gr"]) < 1e-12
+    o = P.observables(shape, U, E)
+    assert o[9] <= 1e-14 * 10 and d["obs_gr"][9] <= 1e-13
+
+
+@pytest.mark.parametrize("nc", [2, 3])
+def test_observables_of_inputs(oracle_port, nc):
+    P = oracle_port[nc]
+    d = load(f"ref_states_su{nc}.npz")
+    shape = tuple(d["shape"])
+    o = P.observables(shape, d["U0"], d["E0"])
+    r = d["obs_0"]
+    for k in range(14):
+        if k == 14:
+            continue
+        assert abs(o[k] - r[k]) < 1e-12 * max(1.0, abs(r[k])), oracle.OBS_FIELDS[k]
+
+
+def test_config0_initial_state_and_series(oracle_port):
+    """BASELINE config 0 (SU(2) 16^3): the oracle's IC equals the reference's, and the
+    first 100 steps of the energy series agree pointwise."""
+    P = oracle_port[2]
+    d = load("ref_c0_su2_16.npz")
+    shape = (16, 16, 16)
+    U, E = oracle.empty_fields(2, shape)
+    P.set_zero(shape, U, E)
+    P.gaussian_efield(shape, E, 1.0 / np.sqrt(2.0), 1)
+    P.gauss_restore(shape, U, E, 1e-14, 10000)
+    assert rel(E, d["E_ic"]) < 1e-12
+    s = d["series"]
+    o = P.observables(shape, U, E)
+    assert abs(o[0] - s[0][0]) < 1e-12
+    for rec in range(1, 11):  # 10 records = 100 steps
+        P.leapfrog(shape, U, E, 0.05, 10)
+        o = P.observables(shape, U, E)
+        assert abs(o[0] - s[rec][0]) < 1e-10 * s[rec][0]
+        assert abs(o[13] - s[rec][13]) < 1e-8 * max(1.0, abs(s[rec][13]))

@@ -1,0 +1,143 @@
+"""Host-side checks of the device arithmetic (no GPU needed).
+
+* Philox4x32-10 against the published known-answer vectors (Salmon et al.,
+  SC'11, Random123 distribution), in the oracle and in the device code.
+* The per-site device functions, instantiated on the host by the test-only
+  build (libtcym_hostcheck.so), against the FP64 oracle: FP64 formats to
+  1e-12, FP32 formats to 1e-5 (the device-path tolerances).
+"""
+import numpy as np
+import pytest
+
+import oracle
+from tests import _hostcheck as hc
+
+KAT = [
+    ((0, 0, 0, 0), (0, 0), (0x6627E8D5, 0xE169C58D, 0xBC57AC4C, 0x9B00DBD8)),
+    ((0xFFFFFFFF,) * 4, (0xFFFFFFFF,) * 2, (0x408F276D, 0x41C83B0E, 0xA20BC7C6, 0x6D5451FD)),
+    ((0x243F6A88, 0x85A308D3, 0x13198A2E, 0x03707344), (0xA4093822, 0x299F31D0),
+     (0xD16CFE09, 0x94FDCCEB, 0x5001E420, 0x24126EA1)),
+]
+
+FORMATS = [(2, "f64"), (2, "f32"), (3, "f64"), (3, "f32")]
+TOL = {"f64": 1e-12, "f32": 1e-5}
+
+
+def rel(a, b):
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+
+@pytest.mark.parametrize("ctr,key,out", KAT)
+def test_philox_known_answers(oracle_port, ctr, key, out):
+    assert tuple(oracle_port[2].philox(ctr, key)) == out
+
+
+def test_device_normals_equal_oracle_normals(oracle_port):
+    P = oracle_port[3]
+    for seed, stream, step, site, mu, a in [(3, 0, 0, 0, 0, 0), (3, 0, 17, 4095, 2, 7), (1, 1, 0, 99, 1, 2),
+                                            (2**40 + 5, 2, 2**33 + 1, 123456, 0, 5)]:
+        ref = P.normal(seed, stream, step, site, mu, a)
+        assert abs(hc.normal(seed, stream, step, site, mu, a) - ref) < 1e-15 * max(1, abs(ref))
+        assert abs(hc.normal(seed, stream, step, site, mu, a, single=True) - ref) < 2e-6 * max(1, abs(ref))
+
+
+def test_normal_stream_statistics(oracle_port):
+    P = oracle_port[3]
+    z = np.array([P.normal(9, 0, 0, s, mu, a) for s in range(400) for mu in range(3) for a in range(8)])
+    assert abs(z.mean()) < 0.05 and abs(z.std() - 1.0) < 0.05
+
+
+@pytest.mark.parametrize("nc,prec", FORMATS)
+def test_exponential(oracle_port, nc, prec):
+    P = oracle_port[nc]
+    rng = np.random.default_rng(5)
+    for scale in (1e-6, 1e-3, 0.1, 1.0, 3.0, 10.0):
+        for _ in range(10):
+            al = rng.normal(size=oracle.NA[nc]) * scale
+            c = float(rng.normal())
+            assert np.abs(hc.iexp(nc, prec, c, al) - P.matrix_iexp(c, al)).max() < 10 * TOL[prec]
+
+
+def _state(P, nc, shape, seed):
+    U, E = oracle.empty_fields(nc, shape)
+    P.random_links(shape, U, 0.6, seed)
+    P.gaussian_efield(shape, E, 0.7, seed + 1)
+    return U, E
+
+
+@pytest.mark.parametrize("nc,prec", FORMATS)
+def test_site_step_leapfrog_langevin_flow(oracle_port, nc, prec):
+    P = oracle_port[nc]
+    shape = (4, 5, 6)
+    U, E = _state(P, nc, shape, 3)
+    H = hc.HostLattice(nc, prec, shape)
+    H.upload(U, E)
+    H.leapfrog(0.05, 10)
+    P.leapfrog(shape, U, E, 0.05, 10)
+    Uh, Eh = H.download()
+    assert rel(Uh, U) < TOL[prec] and rel(Eh, E) < TOL[prec]
+    H.langevin(0.02, 1.0, 0.6, 3, 0, 5)
+    P.langevin(shape, U, E, 0.02, 1.0, 0.6, 3, 0, 5)
+    Uh, Eh = H.download()
+    assert rel(Uh, U) < TOL[prec] and rel(Eh, E) < TOL[prec]
+    H.flow(0.02, 3)
+    P.flow(shape, U, E, 0.02, 3, 0)
+    Uh, Eh = H.download()
+    assert rel(Uh, U) < TOL[prec] and rel(Eh, E) < TOL[prec]
+
+
+@pytest.mark.parametrize("nc,prec", FORMATS)
+def test_site_checkerboard_flow(oracle_port, nc, prec):
+    P = oracle_port[nc]
+    shape = (4, 4, 6)
+    U, E = _state(P, nc, shape, 9)
+    H = hc.HostLattice(nc, prec, shape)
+    H.upload(U, E)
+    H.flow_checkerboard(0.05, 2)
+    P.flow_checkerboard(shape, U, 0.05, 2)
+    assert rel(H.download()[0], U) < TOL[prec]
+
+
+@pytest.mark.parametrize("nc,prec", FORMATS)
+def test_site_observables_and_restore(oracle_port, nc, prec):
+    P = oracle_port[nc]
+    shape = (4, 5, 6)
+    U, E = _state(P, nc, shape, 13)
+    H = hc.HostLattice(nc, prec, shape)
+    H.upload(U, E)
+    Ur, Er = H.download()
+    o, r = H.observables(), P.observables(shape, Ur, Er)
+    for k in list(range(14)) + [15]:
+        assert abs(o[k] - r[k]) < TOL[prec] * max(1.0, abs(r[k])), oracle.OBS_FIELDS[k]
+    if prec == "f64":
+        it_h = H.gauss_restore(1e-14, 10000)
+        it_o = P.gauss_restore(shape, U, E, 1e-14, 10000)
+        assert abs(it_h - it_o) <= 1
+        assert rel(H.download()[1], E) < 1e-12
+
+
+@pytest.mark.parametrize("nc", [2, 3])
+def test_reunitarize_restores_group(oracle_port, nc):
+    P = oracle_port[nc]
+    shape = (3, 3, 4)
+    U, E = _state(P, nc, shape, 21)
+    U = U * (1 + 1e-3 * np.random.default_rng(1).normal(size=U.shape))  # drift off the group
+    H = hc.HostLattice(nc, "f64", shape)
+    H.upload(U, E)
+    assert H.observables()[11] > 1e-4
+    H.reunitarize()
+    assert H.observables()[11] < 1e-14
+
+
+@pytest.mark.parametrize("nc", [2, 3])
+def test_initial_conditions(oracle_port, nc):
+    P = oracle_port[nc]
+    shape = (3, 4, 5)
+    U, E = oracle.empty_fields(nc, shape)
+    P.random_links(shape, U, 0.3, 2)
+    P.gaussian_efield(shape, E, 0.5, 1)
+    H = hc.HostLattice(nc, "f64", shape)
+    H.init(2, 0.3, 2)
+    H.init(1, 0.5, 1)
+    Uh, Eh = H.download()
+    assert rel(Eh, E) < 1e-15 and rel(Uh, U) < 1e-13

@@ -104,6 +104,7 @@ def library() -> ctypes.CDLL:
         "tcym_lattice_download": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
         "tcym_lattice_copy": ([ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
         "tcym_lattice_sync": ([ctypes.c_void_p], ctypes.c_int),
+        "tcym_lattice_stream": ([ctypes.c_void_p, c_void_pp], ctypes.c_int),
         "tcym_set_zero": ([ctypes.c_void_p], ctypes.c_int),
         "tcym_gaussian_efield": ([ctypes.c_void_p, ctypes.c_double, ctypes.c_uint64], ctypes.c_int),
         "tcym_random_links": ([ctypes.c_void_p, ctypes.c_double, ctypes.c_uint64], ctypes.c_int),
@@ -214,6 +215,12 @@ class Lattice:
 
     def sync(self):
         self.ctx.check(self.lib.tcym_lattice_sync(self.h))
+
+    def stream_handle(self) -> int:
+        """cudaStream_t of the lattice (for torch.cuda.ExternalStream / event timing)."""
+        p = ctypes.c_void_p()
+        self.ctx.check(self.lib.tcym_lattice_stream(self.h, ctypes.byref(p)))
+        return p.value or 0
 
     # ---------------------------------------------------- initial conditions
     def set_zero(self):

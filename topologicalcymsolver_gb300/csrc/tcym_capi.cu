@@ -292,6 +292,12 @@ extern "C" int tcym_lattice_sync(tcym_lattice lat) {
     return TCYM_OK;
 }
 
+extern "C" int tcym_lattice_stream(tcym_lattice lat, void **stream) {
+    if (!lat || !stream) return TCYM_ERR_ARG;
+    *stream = (void *)lat->stream;
+    return TCYM_OK;
+}
+
 // ------------------------------------------------------- initial conditions
 extern "C" int tcym_set_zero(tcym_lattice lat) {
     if (!lat) return TCYM_ERR_ARG;
