@@ -44,12 +44,12 @@ FALLBACK_HBM_GBS = 6800.0
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=200)
-    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--steps", type=int, default=2000)
+    p.add_argument("--warmup", type=int, default=10)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--size", type=int, default=128)
     p.add_argument("--dt", type=float, default=0.05)
-    p.add_argument("--e2e-steps", type=int, default=5)
+    p.add_argument("--e2e-steps", type=int, default=10)
     p.add_argument("--no-cpu-baseline", action="store_true")
     return p.parse_args()
 
@@ -239,22 +239,21 @@ def run_ours(a):
     # ---- end to end through the C ABI with pinned host buffers
     Uh = torch.empty((V, 3, 18), dtype=torch.float64, pin_memory=True).numpy()
     Eh = torch.empty((V, 3, 8), dtype=torch.float64, pin_memory=True).numpy()
+    Uo = torch.empty((V, 3, 18), dtype=torch.float64, pin_memory=True).numpy()
+    Eo = torch.empty((V, 3, 8), dtype=torch.float64, pin_memory=True).numpy()
     lat.set_reunitarize_period(0)
-    Ut, Et = lat.download()
-    Uh[...] = Ut
-    Eh[...] = Et
-    del Ut, Et
+    lat.download(Uh, Eh)
     n_e2e = max(1, a.e2e_steps)
     lat.upload(Uh, Eh)
     lat.leapfrog(dt, 1)
-    lat.download()  # warm-up of the staging path
+    lat.download(Uo, Eo)  # warm-up of the staging path
     if ws > 1:
         torch.distributed.barrier()
     t0 = time.perf_counter()
     for _ in range(n_e2e):
         lat.upload(Uh, Eh)
         lat.leapfrog(dt, 1)
-        U2, E2 = lat.download()
+        U2, E2 = lat.download(Uo, Eo)
     e2e_t = time.perf_counter() - t0
     if ws > 1:
         t = torch.tensor([e2e_t], device="cuda")

@@ -199,9 +199,10 @@ class Lattice:
     def upload(self, U=None, E=None):
         self.ctx.check(self.lib.tcym_lattice_upload(self.h, _ptr(U), _ptr(E)))
 
-    def download(self):
-        U = np.empty((self.V, 3, NM[self.nc]))
-        E = np.empty((self.V, 3, NA[self.nc]))
+    def download(self, U=None, E=None):
+        """State as reference AoS FP64 arrays; pass preallocated (e.g. pinned) arrays to fill them."""
+        U = np.empty((self.V, 3, NM[self.nc])) if U is None else U
+        E = np.empty((self.V, 3, NA[self.nc])) if E is None else E
         self.ctx.check(self.lib.tcym_lattice_download(self.h, _ptr(U), _ptr(E)))
         return U, E
 
