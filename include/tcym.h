@@ -128,6 +128,24 @@ int tcym_random_links(tcym_lattice lat, double sigma, uint64_t seed);
  * of G is <= tol (reference: 1e-14) or maxit iterations (reference: 10000).
  * iters / final_max may be NULL. */
 int tcym_gauss_restore(tcym_lattice lat, double tol, int maxit, int *iters, double *final_max);
+/* Same restore, run in place on caller-owned device buffers in the AoS FP64 layouts
+ * above, without allocating any memory.  It has no counterpart in the reference.
+ * It is for callers that cannot let a library call cudaMalloc: their device memory is
+ * wholly reserved by their own allocator, or they run a steady-state loop in which
+ * cudaFree's device-wide synchronisation or a cudaMalloc failure cannot happen.
+ * U_aos (read) and E_aos (updated) are device pointers on the current device; `stream`
+ * is a cudaStream_t (NULL = the default stream); iters / final_max as above (may be
+ * NULL); errbuf receives a message on failure (may be NULL).
+ * Scratch is a fixed 8 MiB device array inside libtcym.so, held by every GPU that loads
+ * the library until the process exits.  Lattices whose violation array (NA * V doubles)
+ * exceeds 1,036,272 doubles are rejected with TCYM_ERR_ARG: SU(2) at most 345,424 sites,
+ * SU(3) at most 129,534 sites.
+ * The first call on a device looks up the scratch address for that device (once); make
+ * that first call before any stream capture.  All calls share the one scratch array,
+ * which keeps the last call's contents (each call clears what must start at zero): calls
+ * that overlap on the GPU, from any thread or stream, race and must not be issued. */
+int tcym_gauss_restore_noalloc(int nc, int nx, int ny, int nz, const double *U_aos, double *E_aos, double tol,
+                               int maxit, void *stream, int *iters, double *final_max, char *errbuf, size_t errlen);
 
 /* --------------------------------------------------------------- dynamics */
 /* Dynamics::Update(U,E) (DYNAMICS/Dynamics.cpp:204-218), nsteps times: E update from

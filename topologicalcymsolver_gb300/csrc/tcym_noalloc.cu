@@ -1,0 +1,199 @@
+// Gauss-law restoration on caller-owned device buffers that allocates nothing.
+//
+// Some callers cannot let a library call cudaMalloc.  One kind has its device
+// memory wholly reserved by its own allocator (a framework's caching allocator
+// that has claimed the GPU), so a fresh allocation fails or fragments the
+// pool.  Another kind runs a steady-state loop that must never stall: cudaFree
+// synchronises the whole device, and cudaMalloc can fail at an arbitrary point
+// under memory pressure.  Such a caller already keeps U and E in the
+// reference's AoS FP64 layout in its own device memory and cannot create a
+// tcym lattice, which owns separate buffers.
+//
+// tcym_gauss_restore_noalloc runs the same Gauss-restore kernels as
+// tcym_gauss_restore directly on those buffers.  Its scratch (the FP64
+// violation array, the per-block reduction records and the result block)
+// lives in one file-scope static __device__ array of kNoAllocScratchDoubles
+// doubles (8 MiB).  Every GPU that loads libtcym.so holds this array until the
+// process exits.  Lattices whose violation array does not fit are rejected.
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+
+#include "../../include/tcym.h"
+#include "tcym_kernels.cuh"
+
+namespace tcym {
+
+// storage formats of the reference's AoS FP64 arrays (LATTICE/GaugeLinks.cpp:27-47,
+// LATTICE/ElectricFields.cpp:36-46), used only by this entry point
+enum : int { FMT_SU2_AOS64 = 10, FMT_SU3_AOS64 = 11 };
+
+template <> struct Fmt<FMT_SU2_AOS64> {
+    using T = double;
+    using G = SU2<double>;
+    using Mat = G::Mat;
+    static constexpr int NA = 3;
+    static TCYM_HD Mat load(const void *U, int64_t, int mu, int64_t s) {
+        const double *a = static_cast<const double *>(U) + 4 * (mu + 3 * s);
+        return Mat{{a[0], a[1], a[2], a[3]}};
+    }
+    static TCYM_HD void load_e(const void *E, int64_t, int mu, int64_t s, T *e) {
+        const double *p = static_cast<const double *>(E) + 3 * (mu + 3 * s);
+        e[0] = p[0]; e[1] = p[1]; e[2] = p[2];
+    }
+    static TCYM_HD void store_e(void *E, int64_t, int mu, int64_t s, const T *e) {
+        double *p = static_cast<double *>(E) + 3 * (mu + 3 * s);
+        p[0] = e[0]; p[1] = e[1]; p[2] = e[2];
+    }
+};
+
+template <> struct Fmt<FMT_SU3_AOS64> {
+    using T = double;
+    using G = SU3<double>;
+    using Mat = G::Mat;
+    static constexpr int NA = 8;
+    static TCYM_HD Mat load(const void *U, int64_t, int mu, int64_t s) {
+        const double *a = static_cast<const double *>(U) + 18 * (mu + 3 * s);
+        Mat m;
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) m.m[i][j] = cx<double>{a[2 * (i + 3 * j)], a[2 * (i + 3 * j) + 1]};
+        return m;
+    }
+    static TCYM_HD void load_e(const void *E, int64_t, int mu, int64_t s, T *e) {
+        const double *p = static_cast<const double *>(E) + 8 * (mu + 3 * s);
+        for (int a = 0; a < 8; ++a) e[a] = p[a];
+    }
+    static TCYM_HD void store_e(void *E, int64_t, int mu, int64_t s, const T *e) {
+        double *p = static_cast<double *>(E) + 8 * (mu + 3 * s);
+        for (int a = 0; a < 8; ++a) p[a] = e[a];
+    }
+};
+
+// Scratch layout (doubles): result block | reduction records | violation array
+constexpr int kNoAllocMaxBlocks = 1024;
+constexpr size_t kNoAllocScratchDoubles = size_t(1) << 20;
+constexpr size_t kNoAllocViolationCapacity =
+    kNoAllocScratchDoubles - R_WIDTH - (size_t)P_WIDTH * kNoAllocMaxBlocks;
+
+static __device__ __align__(256) double g_noalloc_scratch[kNoAllocScratchDoubles];
+
+// Device address of g_noalloc_scratch for each device, looked up once per
+// device with that device current (host code may not use the symbol itself).
+static std::mutex g_scratch_mu;
+static double *g_scratch_addr[256];
+
+static cudaError_t scratch_address(int dev, double **out) {
+    std::lock_guard<std::mutex> g(g_scratch_mu);
+    if (dev < 0 || dev >= 256) return cudaErrorInvalidDevice;
+    if (!g_scratch_addr[dev]) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) return e;
+        g_scratch_addr[dev] = static_cast<double *>(p);
+    }
+    *out = g_scratch_addr[dev];
+    return cudaSuccess;
+}
+
+template <int FMT>
+static cudaError_t restore_aos(const Geom &g, const double *U, double *E, double tol, int maxit, double *scratch,
+                               cudaStream_t st, int *iters, double *final_max) {
+    constexpr int NA = Fmt<FMT>::NA;
+    constexpr int TPB = threads_for<FMT>();
+    double *result = scratch;
+    double *partial = scratch + R_WIDTH;
+    double *G = partial + (size_t)P_WIDTH * kNoAllocMaxBlocks;
+    int blocks = grid_for(g.V, kRedThreads);
+    if (blocks > kNoAllocMaxBlocks) blocks = kNoAllocMaxBlocks;
+    // the array keeps the previous call's contents: clear the result block
+    cudaError_t e = cudaMemsetAsync(result, 0, sizeof(double) * R_WIDTH, st);
+    if (e != cudaSuccess) return e;
+    auto deviation = [&](double *gmax) -> cudaError_t {
+        k_gauss_compute<FMT><<<blocks, kRedThreads, 0, st>>>(g, U, E, G, partial);
+        cudaError_t r = cudaGetLastError();
+        if (r != cudaSuccess) return r;
+        if ((r = finalize_obs(partial, blocks, NA, g.V, 0.0, result, st)) != cudaSuccess) return r;
+        if (!gmax) return cudaSuccess;
+        if ((r = cudaMemcpyAsync(gmax, result + R_GMAX, sizeof(double), cudaMemcpyDeviceToHost, st)) != cudaSuccess)
+            return r;
+        return cudaStreamSynchronize(st);
+    };
+    const double gam[3] = {7.0 / 24.0, 7.0 / 48.0, 7.0 / 72.0};
+    double gmax = 0.0;
+    if ((e = deviation(&gmax)) != cudaSuccess) return e;
+    int it = 0;
+    while (it < maxit && gmax > tol) {
+        for (int k = 0; k < 3; ++k) {
+            if ((e = deviation(nullptr)) != cudaSuccess) return e;
+            k_gauss_update<FMT><<<grid_for(g.V, TPB), TPB, 0, st>>>(g, U, E, G, gam[k]);
+            if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        }
+        // maximum of the last deviation, as the reference tests it (GaussRestore.cpp:150)
+        if ((e = cudaMemcpyAsync(&gmax, result + R_GMAX, sizeof(double), cudaMemcpyDeviceToHost, st)) != cudaSuccess)
+            return e;
+        if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
+        ++it;
+        if (!(gmax == gmax) || gmax > 1e300) break;  // non-finite: reported by the caller below
+    }
+    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
+    *iters = it;
+    *final_max = gmax;
+    return cudaSuccess;
+}
+
+}  // namespace tcym
+
+using namespace tcym;
+
+static int noalloc_fail(char *errbuf, size_t errlen, int code, const char *msg) {
+    if (errbuf && errlen) std::snprintf(errbuf, errlen, "%s", msg);
+    return code;
+}
+
+extern "C" int tcym_gauss_restore_noalloc(int nc, int nx, int ny, int nz, const double *U_aos, double *E_aos,
+                                          double tol, int maxit, void *stream, int *iters, double *final_max,
+                                          char *errbuf, size_t errlen) {
+    if (errbuf && errlen) errbuf[0] = '\0';
+    if ((nc != 2 && nc != 3) || nx < 2 || ny < 2 || nz < 2 || !U_aos || !E_aos || maxit < 0)
+        return noalloc_fail(errbuf, errlen, TCYM_ERR_ARG,
+                            "tcym_gauss_restore_noalloc: nc must be 2 or 3, extents >= 2, buffers non-null");
+    const int64_t V = (int64_t)nx * ny * nz;
+    const int64_t need = (int64_t)(nc == 2 ? 3 : 8) * V;
+    if (need > (int64_t)kNoAllocViolationCapacity) {
+        char msg[256];
+        std::snprintf(msg, sizeof(msg),
+                      "tcym_gauss_restore_noalloc: lattice too large for the fixed scratch: the violation array "
+                      "needs %lld doubles, at most %lld fit (SU(2) <= %lld sites, SU(3) <= %lld sites)",
+                      (long long)need, (long long)kNoAllocViolationCapacity,
+                      (long long)(kNoAllocViolationCapacity / 3), (long long)(kNoAllocViolationCapacity / 8));
+        return noalloc_fail(errbuf, errlen, TCYM_ERR_ARG, msg);
+    }
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    double *scratch = nullptr;
+    if (e == cudaSuccess) e = scratch_address(dev, &scratch);
+    if (e != cudaSuccess) {
+        char msg[256];
+        std::snprintf(msg, sizeof(msg), "tcym_gauss_restore_noalloc: scratch address on device %d: %s", dev,
+                      cudaGetErrorString(e));
+        return noalloc_fail(errbuf, errlen, TCYM_ERR_CUDA, msg);
+    }
+    const Geom g{nx, ny, nz, V};
+    int it = 0;
+    double mx = 0.0;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    e = nc == 2 ? restore_aos<FMT_SU2_AOS64>(g, U_aos, E_aos, tol, maxit, scratch, st, &it, &mx)
+                : restore_aos<FMT_SU3_AOS64>(g, U_aos, E_aos, tol, maxit, scratch, st, &it, &mx);
+    if (e != cudaSuccess) {
+        char msg[256];
+        std::snprintf(msg, sizeof(msg), "tcym_gauss_restore_noalloc: %s", cudaGetErrorString(e));
+        return noalloc_fail(errbuf, errlen, TCYM_ERR_CUDA, msg);
+    }
+    if (iters) *iters = it;
+    if (final_max) *final_max = mx;
+    if (!(mx == mx) || mx > 1e300)
+        return noalloc_fail(errbuf, errlen, TCYM_ERR_NONFINITE, "tcym_gauss_restore_noalloc: non-finite violation");
+    return TCYM_OK;
+}
