@@ -50,6 +50,12 @@ enum {
     TCYM_FP32 = 1  /* FP32 storage (SU(3): two rows), FP64 reductions and reunitarisation */
 };
 
+/* E.B operator of the Chern-Simons rate in calibrated flow */
+enum {
+    TCYM_NCS_IMPROVED = 1, /* O(a^2)-improved, the reference's NCsDot default */
+    TCYM_NCS_CLOVER = 2    /* clover (UnimprovedOperators) */
+};
+
 /* gradient-flow sweep order */
 enum {
     TCYM_FLOW_SIMULTANEOUS = 0, /* all links at once, as GradientFlow::StandardUpdate */
@@ -162,12 +168,14 @@ int tcym_update_u(tcym_lattice lat, double dt);
  * stream keyed by (seed, step, site, mu, colour).  The reference has gamma = 1 and
  * beta = 1/T (LangevinDynamics.cpp:23,184-186). */
 int tcym_langevin(tcym_lattice lat, double dt, double gamma, double T, uint64_t seed, uint64_t step0, int nsteps);
-/* GradientFlow::StandardUpdate (calibrate = 0) / CalibrationUpdate (calibrate = 1)
- * (GRADIENTFLOW/GradientFlow.cpp:150-188), nsteps flow steps of size dtau (the
- * reference's DcTau = SqrtDcTauOverSpacing^2), all links at once or checkerboarded.
- * With calibrate, *dncs receives sum dtau/2 [NCsDot(U,F) + NCsDot(U',F)] using the
- * clover operator.  The field array holds the last flow force afterwards, as in the
- * reference.  Checkerboard mode needs even extents. */
+/* GradientFlow::StandardUpdate (calibrate = 0) / CalibrationUpdate (calibrate =
+ * TCYM_NCS_IMPROVED or TCYM_NCS_CLOVER) (GRADIENTFLOW/GradientFlow.cpp:150-188), nsteps
+ * flow steps of size dtau (the reference's DcTau = SqrtDcTauOverSpacing^2), all links at
+ * once or checkerboarded.  With calibrate, *dncs receives sum dtau/2 [NCsDot(U,F) +
+ * NCsDot(U',F)] with the chosen E.B operator (the reference uses the improved one).
+ * In checkerboard mode F is the force of the state before each sweep.  The field array
+ * holds the last flow force afterwards, as in the reference.  Checkerboard mode needs
+ * even extents. */
 int tcym_flow(tcym_lattice lat, double dtau, int nsteps, int mode, int calibrate, double *dncs);
 /* Projects every stored link back onto the group in FP64 (no reference counterpart). */
 int tcym_reunitarize(tcym_lattice lat);
@@ -181,6 +189,9 @@ int tcym_set_reunitarize_period(tcym_lattice lat, int period);
 int tcym_observables(tcym_lattice lat, tcym_obs *out);
 /* UnimprovedOperators::ComputeEDotB (CALC/ChernSimonsOperators.cpp:4-47): sum_x E.B, clover. */
 int tcym_edotb(tcym_lattice lat, double *out);
+/* ImprovedOperators::ComputeEDotB (CALC/ChernSimonsOperators.cpp:72-382): sum_x E.B with
+ * the O(a^2)-improved fields (4 boxes + 8 rectangles, 4-point transported E). */
+int tcym_edotb_improved(tcym_lattice lat, double *out);
 /* Track N_CS during leapfrog/Langevin steps: every `every` steps (0 = off) add
  * every*dt * NCsDot of the new state to a Kahan-compensated FP64 sum on the device. */
 int tcym_ncs_track(tcym_lattice lat, int every);

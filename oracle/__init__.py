@@ -79,6 +79,8 @@ class Port:
         f("observables").argtypes = [_int_p, _dbl_p, _dbl_p, _dbl_p]
         f("edotb_clover").argtypes = [_int_p, _dbl_p, _dbl_p]
         f("edotb_clover").restype = ctypes.c_double
+        f("edotb_improved").argtypes = [_int_p, _dbl_p, _dbl_p]
+        f("edotb_improved").restype = ctypes.c_double
         f("set_zero").argtypes = [_int_p, _dbl_p, _dbl_p]
         f("gaussian_efield").argtypes = [_int_p, _dbl_p, ctypes.c_double, ctypes.c_uint64]
         f("random_links").argtypes = [_int_p, _dbl_p, ctypes.c_double, ctypes.c_uint64]
@@ -123,6 +125,9 @@ class Port:
 
     def edotb_clover(self, shape, U, E):
         return self._f("edotb_clover")(_n(shape), _p(U), _p(E))
+
+    def edotb_improved(self, shape, U, E):
+        return self._f("edotb_improved")(_n(shape), _p(U), _p(E))
 
     def set_zero(self, shape, U, E):
         self._f("set_zero")(_n(shape), _p(U), _p(E))

@@ -88,7 +88,7 @@ def test_flow_parity(ctx, oracle_port, nc, prec):
     U, E = random_state(P, nc, shape, seed=31)
     lat = tcym.Lattice(ctx, nc, shape, prec)
     lat.upload(U, E)
-    d_gpu = lat.flow(0.02, 5, tcym.FLOW_SIMULTANEOUS, calibrate=True)
+    d_gpu = lat.flow(0.02, 5, tcym.FLOW_SIMULTANEOUS, calibrate=tcym.NCS_IMPROVED)
     d_orc = P.flow(shape, U, E, 0.02, 5, 1)
     Ug, Eg = lat.download()
     assert rel(Ug, U) < TOL[prec]
@@ -118,6 +118,21 @@ def test_observables_parity(ctx, oracle_port, nc, prec):
         assert abs(o[k] - r[k]) <= tol * max(1.0, abs(r[k])), (oracle.OBS_FIELDS[k], o[k], r[k])
     # unitarity: FP32 links carry rounding at 1e-7
     assert abs(o[11] - r[11]) <= (1e-12 if prec == tcym.FP64 else 1e-6)
+
+
+@pytest.mark.parametrize("prec", PREC)
+@pytest.mark.parametrize("nc", GROUPS)
+def test_improved_edotb_parity(ctx, oracle_port, nc, prec):
+    shape = (5, 4, 6)
+    P = oracle_port[nc]
+    U, E = random_state(P, nc, shape, seed=43)
+    lat = tcym.Lattice(ctx, nc, shape, prec)
+    lat.upload(U, E)
+    U, E = lat.download()
+    ref = P.edotb_improved(shape, U, E)
+    tol = 1e-12 if prec == tcym.FP64 else 1e-5
+    assert abs(lat.edotb_improved() - ref) < tol * max(1.0, abs(ref))
+    assert abs(lat.edotb() - P.edotb_clover(shape, U, E)) < tol * max(1.0, abs(ref))
 
 
 @pytest.mark.parametrize("nc", GROUPS)

@@ -47,7 +47,7 @@ def test_states_leapfrog(oracle_port, nc):
         assert rel(E, d["E_" + tag]) < tol
         o = P.observables(shape, U, E)
         r = d["obs_" + tag]
-        for k in range(14):
+        for k in range(15):
             assert abs(o[k] - r[k]) < 1e-9 * max(1.0, abs(r[k])), (tag, oracle.OBS_FIELDS[k])
 
 
@@ -71,10 +71,13 @@ def test_states_flow_and_calibration(oracle_port, nc):
     P.flow(shape, U, E, 0.02, 10, 0)
     assert rel(U, d["U_fl10"]) < 1e-12
     assert rel(E, d["E_fl10"]) < 1e-12
-    # the reference's calibration uses the O(a^2)-improved E.B: compare the state only,
-    # and the clover E.B of the flowed state through the observables
     o = P.observables(shape, U, E)
-    assert abs(o[13] - d["obs_fl10"][13]) < 1e-10 * max(1.0, abs(d["obs_fl10"][13]))
+    for k in (13, 14):  # clover and O(a^2)-improved E.B of the flowed state
+        assert abs(o[k] - d["obs_fl10"][k]) < 1e-10 * max(1.0, abs(d["obs_fl10"][k]))
+    # CalibrationUpdate's Delta N_CS with the reference's NCsDot (improved operator)
+    U, E = d["U0"].copy(), d["E0"].copy()
+    dn = P.flow(shape, U, E, 0.02, 10, 1)
+    assert abs(dn - float(d["dncs_fl10"])) < 1e-12 * max(1.0, abs(float(d["dncs_fl10"])))
 
 
 @pytest.mark.parametrize("nc", [2, 3])
@@ -96,9 +99,7 @@ def test_observables_of_inputs(oracle_port, nc):
     shape = tuple(d["shape"])
     o = P.observables(shape, d["U0"], d["E0"])
     r = d["obs_0"]
-    for k in range(14):
-        if k == 14:
-            continue
+    for k in range(15):
         assert abs(o[k] - r[k]) < 1e-12 * max(1.0, abs(r[k])), oracle.OBS_FIELDS[k]
 
 

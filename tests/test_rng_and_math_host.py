@@ -116,6 +116,18 @@ def test_site_observables_and_restore(oracle_port, nc, prec):
         assert rel(H.download()[1], E) < 1e-12
 
 
+@pytest.mark.parametrize("nc,prec", FORMATS)
+def test_site_improved_edotb(oracle_port, nc, prec):
+    P = oracle_port[nc]
+    shape = (4, 5, 6)
+    U, E = _state(P, nc, shape, 17)
+    H = hc.HostLattice(nc, prec, shape)
+    H.upload(U, E)
+    Ur, Er = H.download()
+    ref = P.edotb_improved(shape, Ur, Er)
+    assert abs(H.observables(mask=16)[13] - ref) < TOL[prec] * max(1.0, abs(ref))
+
+
 @pytest.mark.parametrize("nc", [2, 3])
 def test_reunitarize_restores_group(oracle_port, nc):
     P = oracle_port[nc]

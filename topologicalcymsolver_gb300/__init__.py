@@ -22,10 +22,11 @@ import numpy as np
 from . import build as _build
 
 __all__ = ["Context", "Lattice", "Observables", "TcymError", "FP32", "FP64", "FLOW_SIMULTANEOUS",
-           "FLOW_CHECKERBOARD", "library", "NM", "NA"]
+           "FLOW_CHECKERBOARD", "NCS_IMPROVED", "NCS_CLOVER", "library", "NM", "NA"]
 
 FP64, FP32 = 0, 1
 FLOW_SIMULTANEOUS, FLOW_CHECKERBOARD = 0, 1
+NCS_IMPROVED, NCS_CLOVER = 1, 2  # E.B operator of calibrated flow
 NM = {2: 4, 3: 18}   # doubles per link in the reference AoS layout
 NA = {2: 3, 3: 8}    # algebra components
 
@@ -120,6 +121,7 @@ def library() -> ctypes.CDLL:
         "tcym_set_reunitarize_period": ([ctypes.c_void_p, ctypes.c_int], ctypes.c_int),
         "tcym_observables": ([ctypes.c_void_p, ctypes.POINTER(_Obs)], ctypes.c_int),
         "tcym_edotb": ([ctypes.c_void_p, _dp], ctypes.c_int),
+        "tcym_edotb_improved": ([ctypes.c_void_p, _dp], ctypes.c_int),
         "tcym_ncs_track": ([ctypes.c_void_p, ctypes.c_int], ctypes.c_int),
         "tcym_ncs_get": ([ctypes.c_void_p, _dp], ctypes.c_int),
         "tcym_ncs_reset": ([ctypes.c_void_p], ctypes.c_int),
@@ -251,7 +253,8 @@ class Lattice:
     def langevin(self, dt: float, gamma: float, T: float, seed: int, step0: int, nsteps: int = 1):
         self.ctx.check(self.lib.tcym_langevin(self.h, dt, gamma, T, seed, step0, nsteps))
 
-    def flow(self, dtau: float, nsteps: int = 1, mode: int = FLOW_SIMULTANEOUS, calibrate: bool = False) -> float:
+    def flow(self, dtau: float, nsteps: int = 1, mode: int = FLOW_SIMULTANEOUS, calibrate: int = 0) -> float:
+        """calibrate: 0 none, NCS_IMPROVED (the reference's NCsDot) or NCS_CLOVER; returns Delta N_CS."""
         d = ctypes.c_double()
         self.ctx.check(self.lib.tcym_flow(self.h, dtau, nsteps, mode, int(calibrate), ctypes.byref(d)))
         return d.value
@@ -274,6 +277,11 @@ class Lattice:
     def edotb(self) -> float:
         d = ctypes.c_double()
         self.ctx.check(self.lib.tcym_edotb(self.h, ctypes.byref(d)))
+        return d.value
+
+    def edotb_improved(self) -> float:
+        d = ctypes.c_double()
+        self.ctx.check(self.lib.tcym_edotb_improved(self.h, ctypes.byref(d)))
         return d.value
 
     def ncs_track(self, every: int = 1):

@@ -446,8 +446,12 @@ extern "C" int tcym_update_u(tcym_lattice lat, double dt) {
 }
 
 extern "C" int tcym_flow(tcym_lattice lat, double dtau, int nsteps, int mode, int calibrate, double *dncs) {
-    if (!lat || nsteps < 0 || (mode != TCYM_FLOW_SIMULTANEOUS && mode != TCYM_FLOW_CHECKERBOARD)) return TCYM_ERR_ARG;
+    if (!lat || nsteps < 0 || (mode != TCYM_FLOW_SIMULTANEOUS && mode != TCYM_FLOW_CHECKERBOARD) || calibrate < 0 ||
+        calibrate > 2)
+        return TCYM_ERR_ARG;
     tcym_ctx ctx = lat->ctx;
+    // NCsDot operator: the reference's default is the O(a^2)-improved one (ChernSimonsDerivative.cpp:44)
+    const int op = calibrate == TCYM_NCS_CLOVER ? OBS_EDOTB : OBS_EDOTB_IMP;
     cudaSetDevice(ctx->device);
     if (mode == TCYM_FLOW_CHECKERBOARD && ((lat->g.nx | lat->g.ny | lat->g.nz) & 1)) {
         tcym_set_error(ctx, "tcym_flow: checkerboard sweeps need even extents");
@@ -468,7 +472,7 @@ extern "C" int tcym_flow(tcym_lattice lat, double dtau, int nsteps, int mode, in
                                               lat->stream)));
         }
         if (calibrate) {
-            if ((r = tcym_reduce(lat, OBS_EDOTB, 0.0))) return r;
+            if ((r = tcym_reduce(lat, op, 0.0))) return r;
             if ((r = fetch_result(lat))) return r;
             acc += 0.5 * dtau * inv8pi2 * lat->host_result[R_EDB];
         }
@@ -480,7 +484,7 @@ extern "C" int tcym_flow(tcym_lattice lat, double dtau, int nsteps, int mode, in
                     DISPATCH(lat->fmt, CK(L::flow_cb(lat->g, lat->U[lat->cur], p, mu, c.fc, c.cnu, c.uc, lat->stream)));
         }
         if (calibrate) {
-            if ((r = tcym_reduce(lat, OBS_EDOTB, 0.0))) return r;
+            if ((r = tcym_reduce(lat, op, 0.0))) return r;
             if ((r = fetch_result(lat))) return r;
             acc += 0.5 * dtau * inv8pi2 * lat->host_result[R_EDB];
         }
@@ -539,6 +543,16 @@ extern "C" int tcym_edotb(tcym_lattice lat, double *out) {
     if (!lat || !out) return TCYM_ERR_ARG;
     cudaSetDevice(lat->ctx->device);
     int r = tcym_reduce(lat, OBS_EDOTB, 0.0);
+    if (r) return r;
+    if ((r = fetch_result(lat))) return r;
+    *out = lat->host_result[R_EDB];
+    return TCYM_OK;
+}
+
+extern "C" int tcym_edotb_improved(tcym_lattice lat, double *out) {
+    if (!lat || !out) return TCYM_ERR_ARG;
+    cudaSetDevice(lat->ctx->device);
+    int r = tcym_reduce(lat, OBS_EDOTB_IMP, 0.0);
     if (r) return r;
     if ((r = fetch_result(lat))) return r;
     *out = lat->host_result[R_EDB];

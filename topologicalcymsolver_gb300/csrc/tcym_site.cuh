@@ -160,13 +160,100 @@ TCYM_HD void clover_leaves(const void *U, int64_t V, const Nbhd &nb, int mu, int
     Q[3] = G::mul(G::template mulx<true, true>(a, b), G::mul(c, d));
 }
 
+// Site at (x,y,z) + (dx,dy,dz) with periodic wrap, offsets in [-2, 2].
+TCYM_HD int64_t site_offset(const Geom &g, int x, int y, int z, int dx, int dy, int dz) {
+    int a = x + dx, b = y + dy, c = z + dz;
+    a = a < 0 ? a + g.nx : (a >= g.nx ? a - g.nx : a);
+    b = b < 0 ? b + g.ny : (b >= g.ny ? b - g.ny : b);
+    c = c < 0 ? c + g.nz : (c >= g.nz ? c - g.nz : c);
+    a = a < 0 ? a + g.nx : (a >= g.nx ? a - g.nx : a);  // extents of 2 wrap twice
+    b = b < 0 ? b + g.ny : (b >= g.ny ? b - g.ny : b);
+    c = c < 0 ? c + g.nz : (c >= g.nz ? c - g.nz : c);
+    return (int64_t)a + (int64_t)g.nx * ((int64_t)b + (int64_t)g.ny * c);
+}
+
+// Product of links around a closed path from (x,y,z): step +(d+1) moves along
+// U_d, step -(d+1) moves back along U_d^dag.
+template <class F, int NS>
+TCYM_HD typename F::Mat path_product(const void *U, const Geom &g, int x, int y, int z, const int (&steps)[NS]) {
+    using G = typename F::G;
+    typename F::Mat acc = G::identity();
+    int p[3] = {0, 0, 0};
+#pragma unroll
+    for (int k = 0; k < NS; ++k) {
+        const int d = (steps[k] > 0 ? steps[k] : -steps[k]) - 1;
+        if (steps[k] > 0) {
+            acc = G::mul(acc, F::load(U, g.V, d, site_offset(g, x, y, z, p[0], p[1], p[2])));
+            p[d] += 1;
+        } else {
+            p[d] -= 1;
+            acc = G::template mulx<false, true>(acc, F::load(U, g.V, d, site_offset(g, x, y, z, p[0], p[1], p[2])));
+        }
+    }
+    return acc;
+}
+
+// O(a^2)-improved E.B at one site, ImprovedOperators::ComputeEDotB
+// (CALC/ChernSimonsOperators.cpp:72-382), written with loops from x:
+//   B_i = 2 proj(5/12 sum(4 boxes) - 1/24 sum(8 rectangles)) in the plane (i+1, i+2)
+//   E_i = -1/12 Ad(U_i(x)) E_i(x+i) + 7/12 E_i(x) + 7/12 Ad^-1(U_i(x-i)) E_i(x-i)
+//         - 1/12 Ad^-1(U_i(x-2i) U_i(x-i)) E_i(x-2i)
+// (the reference builds the off-site loops at their own corner and transports
+// them to x, :53-62 and :226-318; the loops from x are the same matrices).
+template <class F> TCYM_HD double site_edotb_improved(const Geom &g, const void *U, const void *E, int64_t s) {
+    using G = typename F::G;
+    using T = typename F::T;
+    using M = typename F::Mat;
+    constexpr int NA = F::NA;
+    const int x = (int)(s % g.nx), y = (int)((s / g.nx) % g.ny), z = (int)(s / ((int64_t)g.nx * g.ny));
+    double sum = 0.0;
+#pragma unroll 1
+    for (int i = 0; i < 3; ++i) {
+        const int J = (i + 1) % 3 + 1, K = (i + 2) % 3 + 1;
+        const int b0[4] = {J, K, -J, -K}, b1[4] = {K, -J, -K, J}, b2[4] = {-K, J, K, -J}, b3[4] = {-J, -K, J, K};
+        const int r0[6] = {J, J, K, -J, -J, -K}, r1[6] = {J, K, K, -J, -K, -K}, r2[6] = {K, -J, -J, -K, J, J},
+                  r3[6] = {K, K, -J, -K, -K, J}, r4[6] = {-J, -J, -K, J, J, K}, r5[6] = {-J, -K, -K, J, K, K},
+                  r6[6] = {-K, J, J, K, -J, -J}, r7[6] = {-K, -K, J, K, K, -J};
+        M boxes = G::add(G::add(path_product<F>(U, g, x, y, z, b0), path_product<F>(U, g, x, y, z, b1)),
+                         G::add(path_product<F>(U, g, x, y, z, b2), path_product<F>(U, g, x, y, z, b3)));
+        M rects = G::add(G::add(path_product<F>(U, g, x, y, z, r0), path_product<F>(U, g, x, y, z, r1)),
+                         G::add(path_product<F>(U, g, x, y, z, r2), path_product<F>(U, g, x, y, z, r3)));
+        rects = G::add(rects, G::add(G::add(path_product<F>(U, g, x, y, z, r4), path_product<F>(U, g, x, y, z, r5)),
+                                     G::add(path_product<F>(U, g, x, y, z, r6), path_product<F>(U, g, x, y, z, r7))));
+        M avg = G::add(G::scale(T(5.0 / 12.0), boxes), G::scale(T(-1.0 / 24.0), rects));
+        T b[NA];
+        G::proj(avg, b);
+        int d[3];
+        unit(i, d);
+        const int64_t sp = site_offset(g, x, y, z, d[0], d[1], d[2]);
+        const int64_t sm = site_offset(g, x, y, z, -d[0], -d[1], -d[2]);
+        const int64_t sm2 = site_offset(g, x, y, z, -2 * d[0], -2 * d[1], -2 * d[2]);
+        T e0[NA], ep[NA], em[NA], em2[NA], t1[NA], t2[NA], t3[NA];
+        F::load_e(E, g.V, i, s, e0);
+        F::load_e(E, g.V, i, sp, ep);
+        F::load_e(E, g.V, i, sm, em);
+        F::load_e(E, g.V, i, sm2, em2);
+        G::adjoint(F::load(U, g.V, i, s), ep, t1);
+        M um = F::load(U, g.V, i, sm);
+        G::inverse_adjoint(um, em, t2);
+        G::inverse_adjoint(G::mul(F::load(U, g.V, i, sm2), um), em2, t3);
+        for (int a = 0; a < NA; ++a) {
+            double ei = -(1.0 / 12.0) * (double)t1[a] + (7.0 / 12.0) * (double)e0[a] + (7.0 / 12.0) * (double)t2[a] -
+                        (1.0 / 12.0) * (double)t3[a];
+            sum += ei * 2.0 * (double)b[a];
+        }
+    }
+    return sum;
+}
+
 // Everything the observables reduce, for one site (FP64 accumulators):
 //   esq[mu]   sum_a E^a_mu(x)^2                        (BulkObservables.cpp:99-130)
 //   bsq[i]    4 Re tr(1 - P_jk(x)), (i,j,k) cyclic      (BulkObservables.cpp:55-88)
 //   g[a]      Gauss violation G^a(x)                    (CALC/GaussViolation.cpp:13-23)
 //   un[mu]    ||U_mu U_mu^dag - 1||                     (UnitarityViolation.cpp:13-51)
 //   edotb     sum_i E_i^clover . B_i^clover             (ChernSimonsOperators.cpp:4-47)
-enum ObsMask : int { OBS_BULK = 1, OBS_GAUSS = 2, OBS_UNIT = 4, OBS_EDOTB = 8, OBS_ALL = 15 };
+// OBS_EDOTB_IMP puts the O(a^2)-improved E.B in the edotb slot instead of the clover one.
+enum ObsMask : int { OBS_BULK = 1, OBS_GAUSS = 2, OBS_UNIT = 4, OBS_EDOTB = 8, OBS_ALL = 15, OBS_EDOTB_IMP = 16 };
 
 template <class F> struct SiteObs {
     double esq[3], bsq[3], g[F::NA], un[3], edotb;
@@ -183,6 +270,10 @@ TCYM_HD void site_observables(const Geom &g, const void *U, const void *E, int m
     for (int mu = 0; mu < 3; ++mu) { o.esq[mu] = 0; o.bsq[mu] = 0; o.un[mu] = 0; }
     for (int a = 0; a < NA; ++a) o.g[a] = 0;
     o.edotb = 0;
+    if (mask & OBS_EDOTB_IMP) {
+        o.edotb = site_edotb_improved<F>(g, U, E, s);
+        mask &= ~(OBS_EDOTB | OBS_EDOTB_IMP);
+    }
     T et[3][NA];  // U_mu^dag(x-mu) E_mu(x-mu) U_mu(x-mu): shared by Gauss and clover E
     if (mask & (OBS_GAUSS | OBS_EDOTB)) {
         for (int mu = 0; mu < 3; ++mu) {
