@@ -85,8 +85,8 @@ def library() -> ctypes.CDLL:
     global _LIB
     if _LIB is not None:
         return _LIB
-    path = _build.LIB
-    if not os.path.exists(path) or os.environ.get("TCYM_REBUILD"):
+    path = os.environ.get("TCYM_LIBRARY", _build.LIB)  # another build of libtcym.so, if given
+    if path == _build.LIB and (not os.path.exists(path) or os.environ.get("TCYM_REBUILD")):
         _build.build_library()
     L = ctypes.CDLL(path)
     c_void_pp = ctypes.POINTER(ctypes.c_void_p)

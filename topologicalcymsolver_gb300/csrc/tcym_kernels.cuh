@@ -26,6 +26,11 @@ enum : int {
 constexpr int kThreadsSU2 = 256;
 constexpr int kThreadsSU3 = 128;
 constexpr int kRedThreads = 256;
+// Resident blocks per SM requested for the SU(3) step (register cap = 65536 / (blocks * threads)).
+#ifndef TCYM_SU3_STEP_MINBLOCKS
+#define TCYM_SU3_STEP_MINBLOCKS 5
+#endif
+template <int FMT> constexpr int min_blocks_for() { return Fmt<FMT>::NA == 3 ? 1 : TCYM_SU3_STEP_MINBLOCKS; }
 
 template <int FMT> constexpr int threads_for() { return Fmt<FMT>::NA == 3 ? kThreadsSU2 : kThreadsSU3; }
 
@@ -48,7 +53,7 @@ template <class T> StepCoef<T> coef_cast(const StepCoef<double> &c) {
 
 // ------------------------------------------------------------------ kernels
 template <int FMT, bool DO_E, bool DO_U>
-__global__ void __launch_bounds__(threads_for<FMT>()) k_step(Geom g, const void *Uin, void *Uout, void *E,
+__global__ void __launch_bounds__(threads_for<FMT>(), min_blocks_for<FMT>()) k_step(Geom g, const void *Uin, void *Uout, void *E,
                                                              StepCoef<typename Fmt<FMT>::T> c) {
     int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= g.V) return;
@@ -57,7 +62,7 @@ __global__ void __launch_bounds__(threads_for<FMT>()) k_step(Geom g, const void 
 
 // sites of parity p, for even extents: t -> (x, row) with x of the right parity
 template <int FMT>
-__global__ void __launch_bounds__(threads_for<FMT>()) k_flow_cb(Geom g, void *U, int parity, int mu,
+__global__ void __launch_bounds__(threads_for<FMT>(), min_blocks_for<FMT>()) k_flow_cb(Geom g, void *U, int parity, int mu,
                                                                 typename Fmt<FMT>::T fc0, typename Fmt<FMT>::T fc1,
                                                                 typename Fmt<FMT>::T fc2, typename Fmt<FMT>::T cn0,
                                                                 typename Fmt<FMT>::T cn1, typename Fmt<FMT>::T cn2,

@@ -130,6 +130,9 @@ template <class T> struct SU2 {
         return w;
     }
     static TCYM_HD Mat mul(const Mat &a, const Mat &b) { return mulx<false, false>(a, b); }
+    // product of group elements (same as mulx for SU(2))
+    template <bool DA, bool DB> static TCYM_HD Mat mulu(const Mat &a, const Mat &b) { return mulx<DA, DB>(a, b); }
+    static TCYM_HD Mat iexp_mul(T c, const T *e, const Mat &u) { return mul(iexp(c, e), u); }
     // proj(u * a) for the force: Re tr(i t^k (u a)) = -(u a)_k
     static TCYM_HD void proj_mul(const Mat &u, const Mat &a, T *out) {
         Mat w = mulx<false, false>(u, a);
@@ -232,6 +235,31 @@ template <class T> struct SU3 {
         return r;
     }
     static TCYM_HD Mat mul(const Mat &a, const Mat &b) { return mulx<false, false>(a, b); }
+
+    // Product of two SU(3) elements: rows 0 and 1 from the factors, row 2 as
+    // conj(row0 x row1).  When a caller reads only rows 0 and 1 of the result
+    // (or of a factor that is not daggered), the compiler drops the rest.
+    template <bool DA, bool DB> static TCYM_HD Mat mulu(const Mat &a, const Mat &b) {
+        Mat r;
+#pragma unroll
+        for (int i = 0; i < 2; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                cx<T> acc{T(0), T(0)};
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    cx<T> x = DA ? a.m[k][i] : a.m[i][k];
+                    cx<T> y = DB ? b.m[j][k] : b.m[k][j];
+                    if (!DA && !DB) acc = cfma(x, y, acc);
+                    else if (!DA && DB) acc = cfma_nc(x, y, acc);
+                    else if (DA && !DB) acc = cfma_cn(x, y, acc);
+                    else acc = cfma_cc(x, y, acc);
+                }
+                r.m[i][j] = acc;
+            }
+        complete_row2(r);
+        return r;
+    }
 
     // Re tr(i t^a V) for all a, V given by its entries; needs Im of the diagonal and
     // both triangles off the diagonal (SU3/GroupOperations.cpp:108-118 expressions).
@@ -363,6 +391,76 @@ template <class T> struct SU3 {
         return r;
     }
     static TCYM_HD Mat iexp(T c, const T *e) { return iexp_hermitian(algebra_matrix(c, e)); }
+
+    // exp(i c t^a e^a) u for a link update.  In the common case (spectral radius
+    // of Q <= 1/2, no scaling) only rows 0 and 1 of exp(iQ) and of the product
+    // are formed; row 2 of the product is conj(row0 x row1).  Otherwise the
+    // scaled-and-squared exponential is used.
+    static TCYM_HD Mat iexp_mul(T c, const T *e, const Mat &u) {
+        const Mat q = algebra_matrix(c, e);
+        // c1 = tr(Q^2)/2 = sum_ij |Q_ij|^2 / 2
+        const T d0 = q.m[0][0].re, d1 = q.m[1][1].re, d2 = q.m[2][2].re;
+        const T o01 = q.m[0][1].re * q.m[0][1].re + q.m[0][1].im * q.m[0][1].im;
+        const T o02 = q.m[0][2].re * q.m[0][2].re + q.m[0][2].im * q.m[0][2].im;
+        const T o12 = q.m[1][2].re * q.m[1][2].re + q.m[1][2].im * q.m[1][2].im;
+        const T c1 = T(0.5) * (d0 * d0 + d1 * d1 + d2 * d2) + (o01 + o02 + o12);
+        if (c1 * T(4.0 / 3.0) > T(0.25)) return mulu<false, false>(iexp_hermitian(q), u);
+        // rows 0 and 1 of Q^2 (Hermitian Q)
+        cx<T> q2[2][3];
+#pragma unroll
+        for (int i = 0; i < 2; ++i)
+#pragma unroll
+            for (int j = i; j < 3; ++j) {
+                cx<T> acc{T(0), T(0)};
+#pragma unroll
+                for (int k = 0; k < 3; ++k) acc = cfma(q.m[i][k], q.m[k][j], acc);
+                q2[i][j] = acc;
+            }
+        q2[1][0] = conj(q2[0][1]);
+        // c0 = det Q (real for Hermitian Q)
+        const T c0 = d0 * (d1 * d2 - o12) - d1 * o02 - d2 * o01 +
+                     T(2) * (q.m[0][1].re * (q.m[1][2].re * q.m[2][0].re - q.m[1][2].im * q.m[2][0].im) -
+                             q.m[0][1].im * (q.m[1][2].re * q.m[2][0].im + q.m[1][2].im * q.m[2][0].re));
+        T f0r, f0i, f1r, f1i, f2r, f2i;
+        series_coeffs(c0, c1, f0r, f0i, f1r, f1i, f2r, f2i);
+        Mat w;
+#pragma unroll
+        for (int i = 0; i < 2; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                const cx<T> x = q.m[i][j], y = q2[i][j];
+                T re = fma(f1r, x.re, fma(-f1i, x.im, fma(f2r, y.re, -f2i * y.im)));
+                T im = fma(f1r, x.im, fma(f1i, x.re, fma(f2r, y.im, f2i * y.re)));
+                if (i == j) { re += f0r; im += f0i; }
+                w.m[i][j] = cx<T>{re, im};
+            }
+        return mulu<false, false>(w, u);  // reads rows 0 and 1 of w only
+    }
+
+    // f_k of exp(iQ) = f0 + f1 Q + f2 Q^2 for spectral radius <= 1/2: the Taylor
+    // series reduced with Q^3 = c1 Q + c0 (Q^n = a_n + b_n Q + d_n Q^2).
+    static TCYM_HD void series_coeffs(T c0, T c1, T &f0r, T &f0i, T &f1r, T &f1i, T &f2r, T &f2i) {
+        constexpr int N = sizeof(T) == 4 ? 9 : 16;
+        constexpr double inv_fact[17] = {1.0, 1.0, 0.5, 1.0 / 6, 1.0 / 24, 1.0 / 120, 1.0 / 720, 1.0 / 5040,
+                                         1.0 / 40320, 1.0 / 362880, 1.0 / 3628800, 1.0 / 39916800,
+                                         1.0 / 479001600, 1.0 / 6227020800.0, 1.0 / 87178291200.0,
+                                         1.0 / 1307674368000.0, 1.0 / 20922789888000.0};
+        T a = T(1), b = T(0), d = T(0);
+        f0r = T(1); f0i = T(0); f1r = T(0); f1i = T(0); f2r = T(0); f2i = T(0);
+#pragma unroll
+        for (int n = 1; n <= N; ++n) {
+            const T na = d * c0, nb = fma(d, c1, a), nd = b;
+            a = na; b = nb; d = nd;
+            const T fct = T(inv_fact[n]);
+            const T wa = fct * a, wb = fct * b, wd = fct * d;
+            switch (n & 3) {  // i^n = 1, i, -1, -i
+                case 0: f0r += wa; f1r += wb; f2r += wd; break;
+                case 1: f0i += wa; f1i += wb; f2i += wd; break;
+                case 2: f0r -= wa; f1r -= wb; f2r -= wd; break;
+                default: f0i -= wa; f1i -= wb; f2i -= wd; break;
+            }
+        }
+    }
 
     // V (e^a t^a) V^dagger and V^dagger (e^a t^a) V in components
     static TCYM_HD void adjoint(const Mat &v, const T *e, T *out) {

@@ -49,14 +49,15 @@ TCYM_HD typename F::Mat staple_sum(const void *U, int64_t V, const Nbhd &nb, int
         unit(nu, dn);
         const int pm[3] = {dm[0] - dn[0], dm[1] - dn[1], dm[2] - dn[2]};
         const int mn[3] = {-dn[0], -dn[1], -dn[2]};
+        // staples are group elements: mulu forms rows 0 and 1 and rebuilds row 2
         M a1 = F::load(U, V, nu, nb.off(dm));
         M a2 = F::load(U, V, mu, nb.off(dn));
         M a3 = F::load(U, V, nu, nb.at(0, 0, 0));
-        M up = G::template mulx<false, true>(G::template mulx<false, true>(a1, a2), a3);
+        M up = G::template mulu<false, true>(G::template mulu<false, true>(a1, a2), a3);
         M b1 = F::load(U, V, nu, nb.off(pm));
         M b2 = F::load(U, V, mu, nb.off(mn));
         M b3 = F::load(U, V, nu, nb.off(mn));
-        M lo = G::template mulx<false, false>(G::template mulx<true, true>(b1, b2), b3);
+        M lo = G::template mulu<false, false>(G::template mulu<true, true>(b1, b2), b3);
         A = G::add(A, G::scale(cnu[nu], G::add(up, lo)));
     }
     return A;
@@ -98,8 +99,7 @@ TCYM_HD void site_step(const Geom &g, const void *Uin, void *Uout, void *E, cons
             F::store_e(E, V, mu, s, e);
         }
         if (DO_U) {
-            M w = G::iexp(c.uc[mu], e);
-            F::store(Uout, V, mu, s, G::mul(w, u));
+            F::store(Uout, V, mu, s, G::iexp_mul(c.uc[mu], e, u));
         }
     }
 }
@@ -120,8 +120,7 @@ TCYM_HD void link_flow(const Geom &g, void *U, int mu, const typename F::T *fc, 
     G::proj_mul(u, A, f);
 #pragma unroll
     for (int a = 0; a < F::NA; ++a) f[a] *= fc[mu];
-    M w = G::iexp(uc[mu], f);
-    F::store(U, g.V, mu, s, G::mul(w, u));
+    F::store(U, g.V, mu, s, G::iexp_mul(uc[mu], f, u));
 }
 
 // ----------------------------------------------------------------- observables
