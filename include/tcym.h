@@ -198,6 +198,34 @@ int tcym_ncs_track(tcym_lattice lat, int every);
 int tcym_ncs_get(tcym_lattice lat, double *ncs);
 int tcym_ncs_reset(tcym_lattice lat);
 
+/* --------------------------------------------------------------- ensembles */
+/* Many independent lattices advanced together: the trajectories the reference
+ * runs as independent MPI ranks sharing only a seed (SU2Solver.cpp:161-164,
+ * SphaleronSimulation.cpp:571-616).  Members may mix groups, sizes, precisions
+ * and dynamics.  Each step is one persistent batched launch per storage format
+ * present; tcym_ensemble_step captures its chunk of steps as a CUDA graph and
+ * replays it while membership and chunk length are unchanged.  A member's
+ * arithmetic is the same as when it is stepped alone.  While a lattice is a
+ * member, step it only through the ensemble; other calls on it are fine
+ * between ensemble calls (tcym_ensemble_step returns after the work is done). */
+typedef struct tcym_ensemble_s *tcym_ensemble;
+enum { TCYM_DYN_LEAPFROG = 0, TCYM_DYN_LANGEVIN = 1 };
+int tcym_ensemble_create(tcym_ctx ctx, tcym_ensemble *out);
+int tcym_ensemble_destroy(tcym_ensemble ens);
+/* Adds a member with its own dynamics: leapfrog (dt) or Langevin (dt, gamma, T,
+ * noise seed, first noise step).  Members keep the order they were added in. */
+int tcym_ensemble_add(tcym_ensemble ens, tcym_lattice lat, int dynamics, double dt, double gamma, double T,
+                      uint64_t seed, uint64_t step0);
+int tcym_ensemble_remove(tcym_ensemble ens, tcym_lattice lat);
+int tcym_ensemble_size(tcym_ensemble ens, int *n);
+/* Advances every member nsteps steps. */
+int tcym_ensemble_step(tcym_ensemble ens, int nsteps);
+/* Clover E.B of every member (sum_x E.B, member order) in one batched reduction.
+ * With ncs_stride > 0 each member's Kahan N_CS advances by ncs_stride*dt*E.B/(8 pi^2)
+ * (a measurement every ncs_stride steps); ncs receives the running N_CS.  Either
+ * output may be NULL. */
+int tcym_ensemble_measure(tcym_ensemble ens, int ncs_stride, double *edotb, double *ncs);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,148 @@
+// Batched kernels: many independent lattices of one storage format advance in
+// one launch.  A persistent grid walks a flattened list of (member, block)
+// work items; each work item is exactly the block the single-lattice kernel
+// would run, calling the same per-site function with the member's own
+// geometry, buffers and coefficients, so a member's arithmetic does not depend
+// on which other lattices share the launch.
+#pragma once
+
+#include "tcym_kernels.cuh"
+
+namespace tcym {
+
+// One ensemble member as the device sees it.
+template <class T> struct Member {
+    Geom g;
+    void *U[2];
+    void *E;
+    double *result;      // the lattice's device result block (Kahan N_CS lives there)
+    StepCoef<T> c;       // c.step is the member's noise counter at the start of the chunk
+    int cur;             // link buffer holding the state at the start of the chunk
+    int block_begin;     // first step work item of this member
+    int red_begin;       // first reduction work item of this member
+    int red_blocks;      // reduction work items of this member
+    double ncs_dt;       // Kahan increment factor for measurements (0: no N_CS update)
+};
+
+// index of the member owning work item `item` (begins sorted ascending)
+template <class T>
+__device__ __forceinline__ int find_member(const Member<T> *m, int n, int item, bool reduction) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        const int b = reduction ? m[mid].red_begin : m[mid].block_begin;
+        if (b <= item) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+// Step k of a chunk for every member: reads U[cur ^ (k&1)], writes U[cur ^ (k&1) ^ 1].
+template <int FMT>
+__global__ void __launch_bounds__(threads_for<FMT>(), min_blocks_for<FMT>())
+    k_step_batch(const Member<typename Fmt<FMT>::T> *members, int nmembers, int total_blocks, int k) {
+    using T = typename Fmt<FMT>::T;
+    for (int item = blockIdx.x; item < total_blocks; item += gridDim.x) {
+        const int mi = find_member(members, nmembers, item, false);
+        const Member<T> &m = members[mi];
+        const int64_t s = (int64_t)(item - m.block_begin) * blockDim.x + threadIdx.x;
+        if (s < m.g.V) {
+            StepCoef<T> c = m.c;
+            c.step = m.c.step + (uint64_t)k;
+            const int in = m.cur ^ (k & 1);
+            site_step<Fmt<FMT>, true, true>(m.g, m.U[in], m.U[in ^ 1], m.E, c, s);
+        }
+    }
+}
+
+// Observables of every member: one partial record per reduction work item.
+template <int FMT>
+__global__ void __launch_bounds__(kRedThreads)
+    k_observables_batch(const Member<typename Fmt<FMT>::T> *members, int nmembers, int total_blocks, int mask,
+                        double *partial) {
+    using F = Fmt<FMT>;
+    using T = typename F::T;
+    for (int item = blockIdx.x; item < total_blocks; item += gridDim.x) {
+        const int mi = find_member(members, nmembers, item, true);
+        const Member<T> &m = members[mi];
+        double v[P_WIDTH];
+#pragma unroll
+        for (int q = 0; q < P_WIDTH; ++q) v[q] = 0.0;
+        const int64_t s = (int64_t)(item - m.red_begin) * blockDim.x + threadIdx.x;
+        if (s < m.g.V) {
+            SiteObs<F> o;
+            site_observables<F>(m.g, m.U[m.cur], m.E, mask, s, o);
+            for (int q = 0; q < 3; ++q) { v[P_ESQ0 + q] = o.esq[q]; v[P_BSQ0 + q] = o.bsq[q]; }
+            for (int a = 0; a < F::NA; ++a) {
+                v[P_GSQ] += o.g[a] * o.g[a];
+                v[P_GMAX] = fmax(v[P_GMAX], o.g[a]);
+                v[P_GABS] = fmax(v[P_GABS], fabs(o.g[a]));
+            }
+            for (int q = 0; q < 3; ++q) { v[P_USQ] += o.un[q] * o.un[q]; v[P_UMAX] = fmax(v[P_UMAX], o.un[q]); }
+            v[P_EDB] = o.edotb;
+        }
+        // block_partial writes at blockIdx.x: give it the work item's slot instead
+        __shared__ double sh[32][P_WIDTH];
+        const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+        for (int q = 0; q < P_WIDTH; ++q) v[q] = q < P_GMAX ? warp_sum(v[q]) : warp_max(v[q]);
+        if (lane == 0)
+#pragma unroll
+            for (int q = 0; q < P_WIDTH; ++q) sh[w][q] = v[q];
+        __syncthreads();
+        if (threadIdx.x < P_WIDTH) {
+            const int q = threadIdx.x;
+            double r = sh[0][q];
+            for (int i = 1; i < nw; ++i) r = q < P_GMAX ? r + sh[i][q] : fmax(r, sh[i][q]);
+            partial[(int64_t)item * P_WIDTH + q] = r;
+        }
+        __syncthreads();
+    }
+}
+
+// Launchers for one format.
+template <int FMT> struct LaunchBatch {
+    using T = typename Fmt<FMT>::T;
+    static constexpr int TPB = threads_for<FMT>();
+    static int resident_blocks() {
+        int b = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_step_batch<FMT>, TPB, 0);
+        return b > 0 ? b : 1;
+    }
+    static cudaError_t step(const Member<T> *members, int n, int total_blocks, int k, int grid, cudaStream_t st) {
+        k_step_batch<FMT><<<grid, TPB, 0, st>>>(members, n, total_blocks, k);
+        return cudaGetLastError();
+    }
+    static cudaError_t observables(const Member<T> *members, int n, int total_blocks, int mask, double *partial,
+                                   int grid, cudaStream_t st) {
+        k_observables_batch<FMT><<<grid, kRedThreads, 0, st>>>(members, n, total_blocks, mask, partial);
+        return cudaGetLastError();
+    }
+};
+
+// Per-member fixed-order sum of its reduction records into its result block
+// (one block per member); advances its Kahan N_CS by ncs_dt * E.B / (8 pi^2).
+struct MemberReduce {
+    const double *partial;
+    int red_begin, red_blocks, na;
+    int64_t V;
+    double ncs_dt;
+    double *result;
+};
+cudaError_t finalize_members(const MemberReduce *items, int n, double *out, cudaStream_t st);
+
+}  // namespace tcym
+
+// The kernels are instantiated once, in tcym_kern_su2.cu and tcym_kern_su3.cu
+// (which define TCYM_KERNEL_TU); every other unit only refers to them.
+#ifndef TCYM_KERNEL_TU
+namespace tcym {
+extern template struct Launch<FMT_SU2_F32>;
+extern template struct Launch<FMT_SU2_F64>;
+extern template struct Launch<FMT_SU3_F32>;
+extern template struct Launch<FMT_SU3_F64>;
+extern template struct LaunchBatch<FMT_SU2_F32>;
+extern template struct LaunchBatch<FMT_SU2_F64>;
+extern template struct LaunchBatch<FMT_SU3_F32>;
+extern template struct LaunchBatch<FMT_SU3_F64>;
+}  // namespace tcym
+#endif

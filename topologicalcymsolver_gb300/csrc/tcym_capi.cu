@@ -12,7 +12,7 @@
 #include <string>
 
 #include "../../include/tcym.h"
-#include "tcym_kernels.cuh"
+#include "tcym_batch.cuh"
 #include "tcym_internal.h"
 
 using namespace tcym;

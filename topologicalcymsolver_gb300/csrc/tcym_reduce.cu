@@ -1,14 +1,15 @@
 // Fixed-order final reduction of the per-block partial records and the
 // Kahan-compensated N_CS accumulator (FP64, on the device).
-#include "tcym_kernels.cuh"
+#include "tcym_batch.cuh"
 
 namespace tcym {
 
 // One block: thread t sums partials t, t+256, ... in order, then a fixed
 // shared-memory tree combines the 256 thread sums.  The order depends only on
-// the number of partials, never on scheduling.
-__global__ void __launch_bounds__(kRedThreads) k_finalize(const double *partial, int blocks, int na, int64_t V,
-                                                          double ncs_dt, double *res) {
+// the number of partials, never on scheduling.  Thread 0 writes the result
+// block and returns E.B and the N_CS sum through *edb / *ncs when given.
+__device__ void finalize_block(const double *partial, int blocks, int na, int64_t V, double ncs_dt, double *res,
+                               double *edb, double *ncs) {
     __shared__ double sh[kRedThreads][P_WIDTH];
     double v[P_WIDTH];
     for (int k = 0; k < P_WIDTH; ++k) v[k] = 0.0;
@@ -42,18 +43,38 @@ __global__ void __launch_bounds__(kRedThreads) k_finalize(const double *partial,
         res[R_NONFINITE] = bad ? 1.0 : res[R_NONFINITE];
         if (ncs_dt != 0.0) {
             // Kahan: sum += ncs_dt * E.B / (8 pi^2) with running compensation
-            const double inv8pi2 = 0.012665147955292221;  // 1 / (8 pi^2)
+            const double inv8pi2 = 0.125 / (3.14159265358979323846 * 3.14159265358979323846);
             double y = ncs_dt * t[P_EDB] * inv8pi2 - res[R_NCS_COMP];
             double s = res[R_NCS] + y;
             res[R_NCS_COMP] = (s - res[R_NCS]) - y;
             res[R_NCS] = s;
         }
+        if (edb) *edb = res[R_EDB];
+        if (ncs) *ncs = res[R_NCS];
     }
+}
+
+__global__ void __launch_bounds__(kRedThreads) k_finalize(const double *partial, int blocks, int na, int64_t V,
+                                                          double ncs_dt, double *res) {
+    finalize_block(partial, blocks, na, V, ncs_dt, res, nullptr, nullptr);
 }
 
 cudaError_t finalize_obs(const double *partial, int blocks, int na, int64_t V, double ncs_dt, double *result,
                          cudaStream_t st) {
     k_finalize<<<1, kRedThreads, 0, st>>>(partial, blocks, na, V, ncs_dt, result);
+    return cudaGetLastError();
+}
+
+// One block per member; out[2i] = E.B, out[2i+1] = N_CS of member i.
+__global__ void __launch_bounds__(kRedThreads) k_finalize_members(const MemberReduce *items, double *out) {
+    const MemberReduce it = items[blockIdx.x];
+    finalize_block(it.partial + (int64_t)it.red_begin * P_WIDTH, it.red_blocks, it.na, it.V, it.ncs_dt, it.result,
+                   out ? out + 2 * blockIdx.x : nullptr, out ? out + 2 * blockIdx.x + 1 : nullptr);
+}
+
+cudaError_t finalize_members(const MemberReduce *items, int n, double *out, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    k_finalize_members<<<n, kRedThreads, 0, st>>>(items, out);
     return cudaGetLastError();
 }
 
