@@ -51,6 +51,11 @@ def parse():
     p.add_argument("--dt", type=float, default=0.05)
     p.add_argument("--e2e-steps", type=int, default=10)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    # other configurations of the reference's workload, each with its own JSON line:
+    # ensemble = 256 mixed trajectories in batched launches; serve = Poisson request stream
+    p.add_argument("--workload", default="leapfrog", choices=["leapfrog", "ensemble", "serve"])
+    p.add_argument("--requests", type=int, default=100)
+    p.add_argument("--trajectories", type=int, default=256)
     return p.parse_args()
 
 
@@ -300,31 +305,34 @@ def run_reference(a):
     # take the run past a few minutes; then a smaller lattice is the sample
     import oracle
     oracle.build()
-    probe = cpu_leapfrog_rate(L, dt, min_seconds=0.0, max_steps=1)
-    per_step = 3 * L ** 3 / probe["value"]
+
+    def runner(Ls):
+        shape = (Ls, Ls, Ls)
+        P = oracle.Port(3)
+        U, E = oracle.empty_fields(3, shape)
+        P.random_links(shape, U, 0.3, 2)
+        P.gaussian_efield(shape, E, np.sqrt(0.5), 1)
+        if oracle.ref_available(3):  # the reference's own sources, where they were compiled on this host
+            try:
+                R = oracle.Ref(3)
+                R.init(shape)
+                R.set(U, E)
+                return (lambda n: R.leapfrog(dt, n)), "reference"
+            except OSError:
+                pass
+        return (lambda n: P.leapfrog(shape, U, E, dt, n)), "port"
+
+    # one step of the full lattice sizes the sample: at most ~3 minutes in all
+    run, kind = runner(L)
+    t0 = time.perf_counter()
+    run(1)
+    per_step = time.perf_counter() - t0
     Ls = L
     while per_step * (a.steps + a.warmup) > 180.0 and Ls > 16:
         Ls //= 2
         per_step /= 8.0
-    res = cpu_leapfrog_rate(Ls, dt, min_seconds=0.0, max_steps=a.steps + a.warmup)
-    # re-time exactly K steps after W warm-up ones
-    import oracle as _o
-    shape = (Ls, Ls, Ls)
-    P = _o.Port(3)
-    U, E = _o.empty_fields(3, shape)
-    P.random_links(shape, U, 0.3, 2)
-    P.gaussian_efield(shape, E, np.sqrt(0.5), 1)
-    kind = "port"
-    run = lambda n: P.leapfrog(shape, U, E, dt, n)  # noqa: E731
-    if _o.ref_available(3):
-        try:
-            R = _o.Ref(3)
-            R.init(shape)
-            R.set(U, E)
-            run = lambda n: R.leapfrog(dt, n)  # noqa: E731
-            kind = "reference"
-        except OSError:
-            pass
+    if Ls != L:
+        run, kind = runner(Ls)
     run(a.warmup)
     t0 = time.perf_counter()
     run(a.steps)
@@ -334,7 +342,6 @@ def run_reference(a):
     sample = (f"{a.steps} leapfrog steps of an SU(3) {Ls}^3 lattice after {a.warmup} warm-up steps, FP64, "
               f"OpenMP over z on {cores} threads" + ("" if Ls == L else f" (the {L}^3 lattice is the GPU workload; "
                                                                         "same per-link work)"))
-    del res
     return {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": a.steps, "warmup": a.warmup,
             "ms_per_step": el / a.steps * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64", "data": "synthetic", "config": config(L, dt), "impl": "reference",
@@ -345,7 +352,10 @@ def run_reference(a):
 def main():
     a = parse()
     os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count() or 1))
-    if a.impl == "reference":
+    if a.workload != "leapfrog":
+        from topologicalcymsolver_gb300 import workloads
+        out = workloads.run(a.workload, a) if dist_env()[1] == 0 else None
+    elif a.impl == "reference":
         out = run_reference(a)
     else:
         out = run_ours(a)

@@ -226,6 +226,52 @@ int tcym_ensemble_step(tcym_ensemble ens, int nsteps);
  * output may be NULL. */
 int tcym_ensemble_measure(tcym_ensemble ens, int ncs_stride, double *edotb, double *ncs);
 
+/* ------------------------------------------------------------------ serving */
+/* A request loop with continuous batching (the reference's one-trajectory-per-
+ * process drivers, SphaleronSimulation.cpp:571-616, LangevinSimulationSU3.cpp:469-512,
+ * as a service).  A background thread admits requests in arrival order while the
+ * device-memory budget and the slot limit allow, advances all admitted requests
+ * together (an ensemble, `stride` steps per tick), records each request's N_CS
+ * every `stride` steps, and retires finished requests at once, freeing their
+ * memory for the next arrivals.  Initial state of a request: U = 1, E ~ N(0, T)
+ * per component from the Philox field stream of its seed, Gauss-restored.
+ * N_CS is the Kahan sum of stride*dt*NCsDot (clover) sampled at the end of each
+ * tick.  Results do not depend on which other requests share the device. */
+typedef struct tcym_server_s *tcym_server;
+typedef struct {
+    int nc;         /* 2 or 3 */
+    int L;          /* cubic extent */
+    int precision;  /* TCYM_FP32 or TCYM_FP64 */
+    int dynamics;   /* TCYM_DYN_LEAPFROG or TCYM_DYN_LANGEVIN */
+    double dt;      /* time step */
+    double gamma;   /* Langevin damping (ignored for leapfrog) */
+    double T;       /* initial E variance and Langevin temperature */
+    int nsteps;     /* steps; rounded up to a multiple of the server's stride */
+    uint64_t seed;  /* Philox seed of the initial fields and of the noise */
+} tcym_request;
+enum { TCYM_REQ_QUEUED = 0, TCYM_REQ_RUNNING = 1, TCYM_REQ_DONE = 2, TCYM_REQ_FAILED = 3 };
+typedef struct {
+    int queued, active;
+    uint64_t completed, failed;
+    size_t bytes_in_use;
+    double link_updates; /* link-updates performed since creation */
+} tcym_server_info;
+int tcym_server_create(tcym_ctx ctx, size_t hbm_budget_bytes, int max_active, int stride, tcym_server *out);
+/* Stops the loop (running requests are abandoned) and frees everything. */
+int tcym_server_destroy(tcym_server srv);
+/* Queues a request (thread-safe, returns at once).  TCYM_ERR_ADMISSION if it can
+ * never fit the budget. */
+int tcym_server_submit(tcym_server srv, const tcym_request *req, uint64_t *id);
+int tcym_server_status(tcym_server srv, uint64_t id, int *status, int *steps_done);
+/* Waits up to timeout_s for the request to finish: TCYM_OK when done,
+ * TCYM_ERR_TIMEOUT when the time ran out, the request's error when it failed. */
+int tcym_server_wait(tcym_server srv, uint64_t id, double timeout_s);
+/* N_CS series of a finished request as (steps, N_CS) pairs (up to `capacity` pairs),
+ * the number of samples and the completion latency (submission to retirement). */
+int tcym_server_result(tcym_server srv, uint64_t id, double *series, int capacity, int *n_samples,
+                       double *latency_s);
+int tcym_server_stats(tcym_server srv, tcym_server_info *out);
+
 #ifdef __cplusplus
 }
 #endif

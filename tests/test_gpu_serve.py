@@ -1,0 +1,98 @@
+"""The continuous-batching request loop (tcym_server_*).
+
+* a request's N_CS series is bit-identical alone and inside a mix of other
+  requests arriving before and after it;
+* it equals the series of the same trajectory stepped through the lattice API;
+* admission keeps the device-memory budget, admits waiting requests as others
+  finish, and refuses a request that can never fit;
+* failures are handled on the host: a bounded wait times out, and a request
+  whose initial fields are NaN (fault injected through its parameters) fails
+  alone while the others complete.
+"""
+import numpy as np
+import pytest
+
+import topologicalcymsolver_gb300 as tcym
+
+pytestmark = pytest.mark.gpu
+
+GB = 1 << 30
+
+
+def test_series_alone_equals_series_in_mix(ctx):
+    probe = dict(nc=3, L=6, T=0.6, nsteps=100, dynamics=tcym.DYN_LANGEVIN, dt=0.02, gamma=1.0, seed=77)
+    a = tcym.Server(ctx, 4 * GB, stride=20)
+    rid = a.submit(**probe)
+    assert a.wait(rid, 300) == 0
+    alone, _, rc = a.result(rid)
+    assert rc == 0 and alone.shape == (5, 2)
+    a.close()
+    b = tcym.Server(ctx, 4 * GB, stride=20)
+    rng = np.random.default_rng(1)
+    others = []
+    for i in range(6):
+        others.append(b.submit(nc=int(rng.choice([2, 3])), L=int(rng.choice([4, 5, 8])), T=float(rng.uniform(0.3, 1)),
+                               nsteps=int(rng.choice([40, 120, 200])), dynamics=int(rng.integers(0, 2)), seed=i))
+    rid = b.submit(**probe)
+    for i in range(6, 10):
+        others.append(b.submit(nc=2, L=6, T=0.5, nsteps=60, seed=i))
+    assert b.wait(rid, 300) == 0
+    mixed, _, rc = b.result(rid)
+    assert rc == 0
+    assert np.array_equal(alone, mixed)
+    for o in others:
+        assert b.wait(o, 300) == 0
+    b.close()
+
+
+def test_series_equals_lattice_path(ctx):
+    nc, L, T, n, stride = 2, 8, 0.7, 60, 20
+    s = tcym.Server(ctx, 2 * GB, stride=stride)
+    rid = s.submit(nc=nc, L=L, T=T, nsteps=n, dynamics=tcym.DYN_LEAPFROG, dt=0.05, precision=tcym.FP64, seed=5)
+    assert s.wait(rid, 300) == 0
+    series, latency, _ = s.result(rid)
+    s.close()
+    lat = tcym.Lattice(ctx, nc, (L, L, L), tcym.FP64)
+    lat.set_zero()
+    lat.gaussian_efield(np.sqrt(T), 5)
+    lat.gauss_restore(1e-12, 400)
+    lat.ncs_track(stride)
+    lat.ncs_reset()
+    ref = []
+    for k in range(n // stride):
+        lat.leapfrog(0.05, stride)
+        ref.append(lat.ncs())
+    assert np.allclose(series[:, 0], [stride * (k + 1) for k in range(n // stride)])
+    assert np.allclose(series[:, 1], ref, rtol=1e-9, atol=1e-12)
+    assert latency > 0
+
+
+def test_admission_by_memory_budget(ctx):
+    # one SU(3) 16^3 FP32 request needs ~6.8 MB: a 16 MB budget holds two at a time
+    s = tcym.Server(ctx, 16 << 20, stride=10)
+    ids = [s.submit(nc=3, L=16, T=0.5, nsteps=30, seed=i) for i in range(6)]
+    peak = 0
+    for rid in ids:
+        while s.wait(rid, 0.01) == 5:
+            peak = max(peak, s.stats()["bytes_in_use"])
+    assert peak <= 16 << 20
+    assert all(s.result(rid)[2] == 0 for rid in ids)
+    st = s.stats()
+    assert st["completed"] == 6 and st["failed"] == 0 and st["bytes_in_use"] == 0
+    with pytest.raises(tcym.TcymError) as ei:
+        s.submit(nc=3, L=64, T=0.5, nsteps=10)
+    assert ei.value.code == 6
+    s.close()
+
+
+def test_bounded_wait_and_injected_fault(ctx):
+    s = tcym.Server(ctx, 4 * GB, stride=20)
+    slow = s.submit(nc=3, L=24, T=0.5, nsteps=4000, seed=1)
+    assert s.wait(slow, 0.0) == 5  # bounded wait runs out: TCYM_ERR_TIMEOUT
+    bad = s.submit(nc=2, L=6, T=float("nan"), nsteps=40, seed=2)
+    good = s.submit(nc=2, L=6, T=0.5, nsteps=40, seed=3)
+    assert s.wait(bad, 300) == 4  # non-finite initial state: the request fails alone
+    assert s.wait(good, 300) == 0
+    st = s.stats()
+    assert st["failed"] == 1
+    s.close()  # abandons the slow request

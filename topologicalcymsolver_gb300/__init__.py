@@ -76,6 +76,17 @@ class Observables:
         return v
 
 
+class _Request(ctypes.Structure):
+    _fields_ = [("nc", ctypes.c_int), ("L", ctypes.c_int), ("precision", ctypes.c_int), ("dynamics", ctypes.c_int),
+                ("dt", ctypes.c_double), ("gamma", ctypes.c_double), ("T", ctypes.c_double), ("nsteps", ctypes.c_int),
+                ("seed", ctypes.c_uint64)]
+
+
+class _ServerInfo(ctypes.Structure):
+    _fields_ = [("queued", ctypes.c_int), ("active", ctypes.c_int), ("completed", ctypes.c_uint64),
+                ("failed", ctypes.c_uint64), ("bytes_in_use", ctypes.c_size_t), ("link_updates", ctypes.c_double)]
+
+
 _LIB = None
 _dp = ctypes.POINTER(ctypes.c_double)
 
@@ -133,6 +144,17 @@ def library() -> ctypes.CDLL:
         "tcym_ensemble_size": ([ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
         "tcym_ensemble_step": ([ctypes.c_void_p, ctypes.c_int], ctypes.c_int),
         "tcym_ensemble_measure": ([ctypes.c_void_p, ctypes.c_int, _dp, _dp], ctypes.c_int),
+        "tcym_server_create": ([ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int, ctypes.c_int, c_void_pp],
+                               ctypes.c_int),
+        "tcym_server_destroy": ([ctypes.c_void_p], ctypes.c_int),
+        "tcym_server_submit": ([ctypes.c_void_p, ctypes.POINTER(_Request), ctypes.POINTER(ctypes.c_uint64)],
+                               ctypes.c_int),
+        "tcym_server_status": ([ctypes.c_void_p, ctypes.c_uint64, ctypes.POINTER(ctypes.c_int),
+                                ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
+        "tcym_server_wait": ([ctypes.c_void_p, ctypes.c_uint64, ctypes.c_double], ctypes.c_int),
+        "tcym_server_result": ([ctypes.c_void_p, ctypes.c_uint64, _dp, ctypes.c_int, ctypes.POINTER(ctypes.c_int),
+                                _dp], ctypes.c_int),
+        "tcym_server_stats": ([ctypes.c_void_p, ctypes.POINTER(_ServerInfo)], ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -344,6 +366,63 @@ class Ensemble:
     def close(self):
         if self.h:
             self.lib.tcym_ensemble_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_FAILED = 0, 1, 2, 3
+
+
+class Server:
+    """Continuous-batching request loop (tcym_server_*): requests are admitted by
+    device-memory footprint, advanced together and retired as they finish."""
+
+    def __init__(self, ctx: Context, hbm_budget_bytes: int, max_active: int = 512, stride: int = 20):
+        self.ctx, self.lib = ctx, ctx.lib
+        h = ctypes.c_void_p()
+        ctx.check(self.lib.tcym_server_create(ctx.h, hbm_budget_bytes, max_active, stride, ctypes.byref(h)))
+        self.h = h
+
+    def submit(self, nc: int, L: int, T: float, nsteps: int, dynamics: int = DYN_LEAPFROG, dt: float = 0.05,
+               gamma: float = 1.0, precision: int = FP32, seed: int = 0) -> int:
+        r = _Request(nc, L, precision, dynamics, dt, gamma, T, nsteps, seed)
+        i = ctypes.c_uint64()
+        self.ctx.check(self.lib.tcym_server_submit(self.h, ctypes.byref(r), ctypes.byref(i)))
+        return i.value
+
+    def status(self, rid: int):
+        s, n = ctypes.c_int(), ctypes.c_int()
+        self.ctx.check(self.lib.tcym_server_status(self.h, rid, ctypes.byref(s), ctypes.byref(n)))
+        return s.value, n.value
+
+    def wait(self, rid: int, timeout_s: float = 600.0) -> int:
+        """Status code of the bounded wait (0 = done, 5 = timed out, else the request's error)."""
+        return self.lib.tcym_server_wait(self.h, rid, timeout_s)
+
+    def result(self, rid: int):
+        """(series (n, 2) of (steps, N_CS), latency in s, status code)."""
+        n, lat = ctypes.c_int(), ctypes.c_double()
+        rc = self.lib.tcym_server_result(self.h, rid, None, 0, ctypes.byref(n), ctypes.byref(lat))
+        if rc not in (0, 4) and n.value == 0 and lat.value == 0.0:
+            self.ctx.check(rc)
+        buf = np.zeros((max(n.value, 1), 2))
+        rc = self.lib.tcym_server_result(self.h, rid, buf.ctypes.data_as(_dp), n.value, ctypes.byref(n),
+                                         ctypes.byref(lat))
+        return buf[: n.value], lat.value, rc
+
+    def stats(self) -> dict:
+        s = _ServerInfo()
+        self.ctx.check(self.lib.tcym_server_stats(self.h, ctypes.byref(s)))
+        return {k: getattr(s, k) for k, _ in _ServerInfo._fields_}
+
+    def close(self):
+        if self.h:
+            self.lib.tcym_server_destroy(self.h)
             self.h = None
 
     def __del__(self):

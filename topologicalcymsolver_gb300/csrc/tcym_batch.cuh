@@ -43,13 +43,15 @@ __global__ void __launch_bounds__(threads_for<FMT>(), min_blocks_for<FMT>())
     using T = typename Fmt<FMT>::T;
     for (int item = blockIdx.x; item < total_blocks; item += gridDim.x) {
         const int mi = find_member(members, nmembers, item, false);
-        const Member<T> &m = members[mi];
-        const int64_t s = (int64_t)(item - m.block_begin) * blockDim.x + threadIdx.x;
-        if (s < m.g.V) {
-            StepCoef<T> c = m.c;
-            c.step = m.c.step + (uint64_t)k;
-            const int in = m.cur ^ (k & 1);
-            site_step<Fmt<FMT>, true, true>(m.g, m.U[in], m.U[in ^ 1], m.E, c, s);
+        // the member into registers: stores to the fields could otherwise alias the table
+        const Geom g = members[mi].g;
+        const int64_t s = (int64_t)(item - members[mi].block_begin) * blockDim.x + threadIdx.x;
+        if (s < g.V) {
+            StepCoef<T> c = members[mi].c;
+            c.step += (uint64_t)k;
+            const int in = members[mi].cur ^ (k & 1);
+            void *uin = members[mi].U[in], *uout = members[mi].U[in ^ 1], *e = members[mi].E;
+            site_step<Fmt<FMT>, true, true>(g, uin, uout, e, c, s);
         }
     }
 }
@@ -63,14 +65,15 @@ __global__ void __launch_bounds__(kRedThreads)
     using T = typename F::T;
     for (int item = blockIdx.x; item < total_blocks; item += gridDim.x) {
         const int mi = find_member(members, nmembers, item, true);
-        const Member<T> &m = members[mi];
+        const Geom g = members[mi].g;
+        const void *u = members[mi].U[members[mi].cur], *e = members[mi].E;
         double v[P_WIDTH];
 #pragma unroll
         for (int q = 0; q < P_WIDTH; ++q) v[q] = 0.0;
-        const int64_t s = (int64_t)(item - m.red_begin) * blockDim.x + threadIdx.x;
-        if (s < m.g.V) {
+        const int64_t s = (int64_t)(item - members[mi].red_begin) * blockDim.x + threadIdx.x;
+        if (s < g.V) {
             SiteObs<F> o;
-            site_observables<F>(m.g, m.U[m.cur], m.E, mask, s, o);
+            site_observables<F>(g, u, e, mask, s, o);
             for (int q = 0; q < 3; ++q) { v[P_ESQ0 + q] = o.esq[q]; v[P_BSQ0 + q] = o.bsq[q]; }
             for (int a = 0; a < F::NA; ++a) {
                 v[P_GSQ] += o.g[a] * o.g[a];

@@ -292,6 +292,17 @@ extern "C" int tcym_lattice_sync(tcym_lattice lat) {
     return TCYM_OK;
 }
 
+void tcym_lattice_release_scratch(tcym_lattice lat) {
+    if (!lat) return;
+    cudaSetDevice(lat->ctx->device);
+    cudaStreamSynchronize(lat->stream);
+    cudaFree(lat->gauss);
+    cudaFree(lat->staging);
+    lat->gauss = nullptr;
+    lat->staging = nullptr;
+    lat->staging_bytes = 0;
+}
+
 extern "C" int tcym_lattice_stream(tcym_lattice lat, void **stream) {
     if (!lat || !stream) return TCYM_ERR_ARG;
     *stream = (void *)lat->stream;

@@ -45,5 +45,7 @@ size_t tcym_field_bytes(int fmt);
 tcym::StepCoef<double> tcym_coef(const double *a, int mode, double dt, double gamma, double T, uint64_t seed,
                                  uint64_t step);
 int tcym_reduce(tcym_lattice lat, int mask, double ncs_dt);
+// frees the Gauss-restore and AoS staging scratch of a lattice (reallocated on next use)
+void tcym_lattice_release_scratch(tcym_lattice lat);
 int tcym_run_steps(tcym_lattice lat, int mode, double dt, double gamma, double T, uint64_t seed, uint64_t step0,
                    int nsteps);

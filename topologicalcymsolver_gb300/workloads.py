@@ -1,0 +1,199 @@
+"""Workload generators and runners for the batched configurations.
+
+ensemble: 256 independent thermal leapfrog trajectories, each SU(2) or SU(3)
+  (50/50), L uniform in {16, 24, 32, 48}, dt = 0.05, E-field variance T uniform
+  in [0.3, 1.0], fields from the Philox stream of seed 5 + index, Gauss-restored
+  in FP64 to 1e-10, stepped in FP32 storage with FP64 reductions, in batched
+  graph-captured launches (tcym_ensemble_*).  Compared with the same lattices
+  stepped by per-lattice launches and with the plain FP64 path.
+serve: a Poisson request stream at 80% of the measured sustainable throughput;
+  each request: SU(2)/SU(3) 50/50, L uniform over {24, 32, 48, 64, 96, 128}
+  (log-spaced, so uniform in log L), T uniform in [0.3, 1.0], leapfrog or
+  Langevin (gamma = 1) 50/50, steps log-uniform in [1000, 20000], N_CS(t)
+  every 20 steps (tcym_server_*).
+
+Inputs are synthetic: seeded Philox fields with the configurations' distributions.
+"""
+from __future__ import annotations
+
+import math
+import time
+
+import numpy as np
+
+from . import DYN_LANGEVIN, DYN_LEAPFROG, FP32, FP64, Context, Ensemble, Lattice, Server
+
+GB = 1 << 30
+
+
+def ensemble_specs(n: int = 256, seed: int = 5):
+    """(nc, L, T, field seed) of each trajectory."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        nc = 2 if rng.random() < 0.5 else 3
+        L = int(rng.choice([16, 24, 32, 48]))
+        T = float(rng.uniform(0.3, 1.0))
+        out.append((nc, L, T, seed + i))
+    return out
+
+
+def thermal_lattice(ctx: Context, nc: int, L: int, T: float, seed: int, precision: int, tol: float = 1e-10):
+    """U = 1, E ~ N(0, T) Gauss-restored in FP64, stored in `precision`."""
+    ic = Lattice(ctx, nc, (L, L, L), FP64)
+    ic.set_zero()
+    ic.gaussian_efield(math.sqrt(T), seed)
+    ic.gauss_restore(tol, 5000)
+    if precision == FP64:
+        return ic
+    lat = Lattice(ctx, nc, (L, L, L), precision)
+    lat.copy_from(ic)
+    ic.close()
+    return lat
+
+
+def run_ensemble(a):
+    ctx = Context(0)
+    specs = ensemble_specs(a.trajectories)
+    lats = [thermal_lattice(ctx, nc, L, T, s, FP32) for nc, L, T, s in specs]
+    links = sum(3 * L ** 3 for _, L, _, _ in specs)
+    dt = 0.05
+    ens = Ensemble(ctx)
+    for lat in lats:
+        ens.add(lat, dt)
+    chunk = 100
+    ens.step(max(a.warmup, 3))
+    steps = max(chunk, (a.steps // chunk) * chunk)
+    t0 = time.perf_counter()
+    for _ in range(steps // chunk):
+        ens.step(chunk)
+    t_ens = time.perf_counter() - t0
+    rate = links * steps / t_ens
+    # per-lattice launches, bounded samples
+    nseq = 50
+    t0 = time.perf_counter()
+    for _ in range(nseq):
+        for lat in lats:
+            lat.leapfrog(dt, 1)
+            lat.sync()
+    seq_serial = links * nseq / (time.perf_counter() - t0)
+    t0 = time.perf_counter()
+    for _ in range(nseq):
+        for lat in lats:
+            lat.leapfrog(dt, 1)
+    for lat in lats:
+        lat.sync()
+    seq_concurrent = links * nseq / (time.perf_counter() - t0)
+    ens.close()
+    for lat in lats:
+        lat.close()
+    # the plain FP64 path: the same trajectories in FP64 storage, batched
+    lats64 = [thermal_lattice(ctx, nc, L, T, s, FP64) for nc, L, T, s in specs]
+    e64 = Ensemble(ctx)
+    for lat in lats64:
+        e64.add(lat, dt)
+    e64.step(3)
+    n64 = 20
+    t0 = time.perf_counter()
+    e64.step(n64)
+    fp64 = links * n64 / (time.perf_counter() - t0)
+    e64.close()
+    for lat in lats64:
+        lat.close()
+    ctx.close()
+    n_su3 = sum(1 for s in specs if s[0] == 3)
+    return {
+        "metric": "ensemble trajectories/s (256 mixed SU(2)/SU(3) thermal trajectories, 2000 steps each)",
+        "value": a.trajectories * (steps / 2000.0) / t_ens, "unit": "trajectories/s", "higher_is_better": True,
+        "n_gpus": 1, "steps": steps, "warmup": max(a.warmup, 3), "dtype": "f32", "data": "synthetic",
+        "vs_baseline": None, "impl": "ours",
+        "config": {"workload": f"{a.trajectories} trajectories ({n_su3} SU(3)), L in {{16,24,32,48}}, dt=0.05, "
+                               "T in [0.3,1], FP32 storage, FP64 reductions, graph chunks of 100 steps",
+                   "link_updates_per_step": links},
+        "link_updates_per_s": rate,
+        "per_lattice_launches_serialized": seq_serial,
+        "per_lattice_launches_concurrent_streams": seq_concurrent,
+        "fp64_ensemble": fp64,
+        "speedup_vs_serialized_launches": rate / seq_serial,
+        "speedup_vs_concurrent_launches": rate / seq_concurrent,
+        "speedup_vs_fp64": rate / fp64,
+    }
+
+
+def serve_requests(n: int, seed: int = 6):
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        out.append(dict(nc=2 if rng.random() < 0.5 else 3, L=int(rng.choice([24, 32, 48, 64, 96, 128])),
+                        T=float(rng.uniform(0.3, 1.0)),
+                        dynamics=DYN_LANGEVIN if rng.random() < 0.5 else DYN_LEAPFROG,
+                        nsteps=int(round(math.exp(rng.uniform(math.log(1000), math.log(20000))))),
+                        seed=seed * 1000 + i))
+    return out
+
+
+def _work(r, stride=20):
+    return 3 * r["L"] ** 3 * int(math.ceil(r["nsteps"] / stride) * stride)
+
+
+def run_serve(a):
+    ctx = Context(0)
+    reqs = serve_requests(a.requests)
+    dt = {DYN_LEAPFROG: 0.05, DYN_LANGEVIN: 0.02}
+    budget = 200 * GB
+    srv = Server(ctx, budget, max_active=512, stride=20)
+
+    def submit(r):
+        return srv.submit(nc=r["nc"], L=r["L"], T=r["T"], nsteps=r["nsteps"], dynamics=r["dynamics"],
+                          dt=dt[r["dynamics"]], gamma=1.0, precision=FP32, seed=r["seed"])
+
+    # sustainable throughput: a saturating batch drawn from the same distribution
+    sat = serve_requests(min(32, a.requests), seed=60)
+    t0 = time.perf_counter()
+    ids = [submit(r) for r in sat]
+    for i in ids:
+        srv.wait(i, 3600)
+    sustainable = sum(_work(r) for r in sat) / (time.perf_counter() - t0)
+    # Poisson arrivals at 80% of it
+    mean_work = sum(_work(r) for r in reqs) / len(reqs)
+    lam = 0.8 * sustainable / mean_work
+    rng = np.random.default_rng(66)
+    arrivals = np.cumsum(rng.exponential(1.0 / lam, size=len(reqs)))
+    start = time.perf_counter()
+    ids = []
+    for r, ta in zip(reqs, arrivals):
+        delay = start + ta - time.perf_counter()
+        if delay > 0:
+            time.sleep(delay)
+        ids.append(submit(r))
+    lat_s, failed = [], 0
+    for i in ids:
+        rc = srv.wait(i, 7200)
+        series, latency, rc2 = srv.result(i)
+        if rc != 0:
+            failed += 1
+        lat_s.append(latency)
+    makespan = time.perf_counter() - start
+    stats = srv.stats()
+    srv.close()
+    ctx.close()
+    total = sum(_work(r) for r in reqs)
+    return {
+        "metric": "serving: aggregate link-updates/s under a Poisson request stream at 80% of sustainable throughput",
+        "value": total / makespan, "unit": "link-updates/s", "higher_is_better": True, "n_gpus": 1,
+        "dtype": "f32", "data": "synthetic", "vs_baseline": None, "impl": "ours",
+        "config": {"workload": f"{len(reqs)} requests (Poisson, seed 6), SU(2)/SU(3), L in {{24..128}}, "
+                               "T in [0.3,1], leapfrog dt 0.05 / Langevin dt 0.02 gamma 1, steps log-uniform "
+                               "[1000, 20000], N_CS every 20 steps, FP32 storage, budget 200 GiB"},
+        "p50_latency_s": float(np.percentile(lat_s, 50)), "p99_latency_s": float(np.percentile(lat_s, 99)),
+        "requests": len(reqs), "failed": failed, "sustainable_link_updates_per_s": sustainable,
+        "offered_requests_per_s": lam, "makespan_s": makespan, "server_link_updates": stats["link_updates"],
+    }
+
+
+def run(name: str, a):
+    if name == "ensemble":
+        return run_ensemble(a)
+    if name == "serve":
+        return run_serve(a)
+    raise ValueError(name)
