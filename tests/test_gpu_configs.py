@@ -1,0 +1,172 @@
+"""The BASELINE configurations as parity tests (GPU through the C ABI).
+
+config 0: SU(2) 16^3, U = 1, E ~ N(0, 1/2) (seed 1) Gauss-restored, 1000 leapfrog
+  steps at dt 0.05, observables every 10 steps: compared with the reference's own
+  series (tests/golden/ref_c0_su2_16.npz) pointwise over the first 100 steps
+  and, beyond the chaotic horizon, through the conserved energy.
+config 1: SU(3) Langevin 64^3, dt 0.02, gamma 1, T 0.6, links exp(i theta lambda/2)
+  theta ~ N(0, 0.09) (seed 2), E = 0, noise seed 3: pointwise against the FP64
+  oracle fed the identical noise for 100 steps (FP64 <= 1e-10, FP32 <= 1e-5
+  relative), and the Kahan-integrated N_CS over the first 10.
+config 2: leapfrog, then checkerboarded gradient-flow cooling sweeps at
+  dtau 0.02: at 32^3 against the oracle's checkerboard restatement every 10
+  sweeps; at the full 96^3 (2000 leapfrog steps, 500 sweeps) FP32 storage
+  against the FP64 path over the first 30 sweeps, and the energy decaying
+  monotonically over all 500 in both.
+energy: over 10^4 leapfrog steps neither path's mean energy drifts and the
+  FP32 path's stays with the FP64 path's.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+import topologicalcymsolver_gb300 as tcym
+
+pytestmark = pytest.mark.gpu
+
+G = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def rel(a, b):
+    return float(np.abs(a - b).max() / np.abs(b).max())
+
+
+# tolerances: (energies, E.B) relative to max(1, |value|)
+@pytest.mark.parametrize("prec,tol_e,tol_edb", [(tcym.FP64, 1e-10, 1e-8), (tcym.FP32, 2e-5, 2e-3)])
+def test_config0_against_reference_series(ctx, prec, tol_e, tol_edb):
+    d = dict(np.load(os.path.join(G, "ref_c0_su2_16.npz")))
+    s = d["series"]
+    shape = (16, 16, 16)
+    ic = tcym.Lattice(ctx, 2, shape, tcym.FP64)
+    ic.set_zero()
+    ic.gaussian_efield(1.0 / np.sqrt(2.0), 1)
+    ic.gauss_restore(1e-14, 10000)
+    assert rel(ic.download()[1], d["E_ic"]) < 1e-12
+    lat = ic
+    if prec == tcym.FP32:
+        lat = tcym.Lattice(ctx, 2, shape, prec)
+        lat.copy_from(ic)
+    T00 = []
+    for rec in range(len(s)):
+        if rec:
+            lat.leapfrog(float(d["dt"]), int(d["every"]))
+        o = lat.observables()
+        v = o.as_oracle_vector()
+        T00.append(v[0])
+        if rec <= 10:  # the first 100 steps: pointwise
+            for k in (0, 1, 2):
+                assert abs(v[k] - s[rec][k]) <= tol_e * max(1.0, abs(s[rec][k])), (rec, k, v[k], s[rec][k])
+            assert abs(v[13] - s[rec][13]) <= tol_edb * max(1.0, abs(s[rec][13])), (rec, v[13], s[rec][13])
+        assert o.gauss_absmax < (1e-11 if prec == tcym.FP64 else 1e-4)
+        assert o.unit_max < (1e-12 if prec == tcym.FP64 else 1e-5)
+    T00, Tref = np.array(T00), s[:, 0]
+    # beyond the chaotic horizon both conserve the energy: they agree to the leapfrog fluctuation
+    assert np.abs(T00[20:] - Tref[20:]).max() < 5e-3 * Tref.mean()
+    assert abs(T00[-50:].mean() - Tref[-50:].mean()) < 1e-3 * Tref.mean()
+
+
+@pytest.mark.parametrize("prec,tol", [(tcym.FP64, 1e-10), (tcym.FP32, 1e-5)])
+def test_config1_langevin_64_identical_noise(ctx, oracle_port, prec, tol):
+    P = oracle_port[3]
+    shape = (64, 64, 64)
+    U, E = oracle.empty_fields(3, shape)
+    P.random_links(shape, U, 0.3, 2)
+    lat = tcym.Lattice(ctx, 3, shape, prec)
+    lat.random_links(0.3, 2)
+    lat.set_reunitarize_period(0)
+    Ug, _ = lat.download()
+    assert rel(Ug, U) < (1e-13 if prec == tcym.FP64 else 5e-7)
+    if prec == tcym.FP32:  # the oracle starts from the same rounded links
+        U = Ug
+    lat.upload(U, E)
+    lat.ncs_track(1)
+    lat.ncs_reset()
+    dt, ncs, scale = 0.02, 0.0, 0.0
+    for k in range(10):
+        lat.langevin(dt, 1.0, 0.6, 3, k, 1)
+        P.langevin(shape, U, E, dt, 1.0, 0.6, 3, k, 1)
+        edb = P.edotb_clover(shape, U, E)
+        ncs += dt * edb / (8 * np.pi ** 2)
+        scale += dt * abs(edb) / (8 * np.pi ** 2)
+    assert abs(lat.ncs() - ncs) <= 100 * tol * scale + 1e-13, (lat.ncs(), ncs, scale)
+    lat.langevin(dt, 1.0, 0.6, 3, 10, 90)
+    P.langevin(shape, U, E, dt, 1.0, 0.6, 3, 10, 90)
+    Ug, Eg = lat.download()
+    assert rel(Ug, U) < tol and rel(Eg, E) < tol, (rel(Ug, U), rel(Eg, E))
+
+
+def _cooling_input(ctx, shape, nlf, tol=1e-14):
+    lat = tcym.Lattice(ctx, 2, shape, tcym.FP64)
+    lat.set_zero()
+    lat.gaussian_efield(np.sqrt(0.5), 4)
+    lat.gauss_restore(tol, 10000)
+    lat.leapfrog(0.05, nlf)
+    return lat
+
+
+@pytest.mark.parametrize("prec,tol", [(tcym.FP64, 1e-10), (tcym.FP32, 2e-5)])
+def test_config2_cooling_against_oracle(ctx, oracle_port, prec, tol):
+    P = oracle_port[2]
+    shape = (32, 32, 32)
+    src = _cooling_input(ctx, shape, 200)
+    U, E = src.download()
+    lat = tcym.Lattice(ctx, 2, shape, prec)
+    lat.copy_from(src)
+    if prec == tcym.FP32:
+        U, E = lat.download()
+    mags = []
+    for sweep in range(5):
+        lat.flow(0.02, 10, tcym.FLOW_CHECKERBOARD)
+        P.flow_checkerboard(shape, U, 0.02, 10)
+        Ug, _ = lat.download()
+        assert rel(Ug, U) < tol, (sweep, rel(Ug, U))
+        o = lat.observables().as_oracle_vector()
+        r = P.observables(shape, U, E)
+        assert abs(o[2] - r[2]) <= 10 * tol * r[2]
+        mags.append(o[2])
+    assert all(b < a for a, b in zip(mags, mags[1:]))  # cooling lowers the magnetic energy
+
+
+def test_config2_full_size_fp32_tracks_fp64(ctx):
+    shape = (96, 96, 96)
+    l64 = _cooling_input(ctx, shape, 2000, tol=1e-12)
+    l32 = tcym.Lattice(ctx, 2, shape, tcym.FP32)
+    l32.copy_from(l64)
+    m64, m32 = [], []
+    for _ in range(50):  # 500 sweeps, energies every 10
+        for lat, m in ((l64, m64), (l32, m32)):
+            lat.flow(0.02, 10, tcym.FLOW_CHECKERBOARD)
+            m.append(lat.observables().magnetic)
+    m64, m32 = np.array(m64), np.array(m32)
+    # both cool monotonically to below 1% of the first record
+    assert np.all(np.diff(m64) < 0) and np.all(np.diff(m32) < 0)
+    assert m64[-1] < 0.01 * m64[0] and m32[-1] < 0.01 * m32[0]
+    # pointwise over the first 30 sweeps; later the flow nears saddle points whose unstable
+    # directions amplify any difference (FP32 against FP64 grows ~3x per 10 sweeps there)
+    assert np.abs(m32[:3] / m64[:3] - 1).max() < 1e-5, np.abs(m32 / m64 - 1)[:6]
+
+
+def test_energy_drift_fp32_vs_fp64(ctx):
+    shape = (32, 32, 32)
+    l64 = tcym.Lattice(ctx, 3, shape, tcym.FP64)
+    l64.set_zero()
+    l64.gaussian_efield(np.sqrt(0.5), 11)
+    l64.gauss_restore(1e-12, 4000)
+    l64.leapfrog(0.05, 400)  # past the initial transient of B = 0
+    l32 = tcym.Lattice(ctx, 3, shape, tcym.FP32)
+    l32.copy_from(l64)
+    e = {tcym.FP64: [], tcym.FP32: []}
+    for _ in range(200):
+        for lat, key in ((l64, tcym.FP64), (l32, tcym.FP32)):
+            lat.leapfrog(0.05, 50)
+            e[key].append(lat.observables().T00)
+    e64, e32 = np.array(e[tcym.FP64]), np.array(e[tcym.FP32])
+    # 10^4 steps: the mean energy does not drift between halves, in either precision,
+    # and the FP32 path's mean stays with the FP64 path's (the bounds are a few
+    # standard errors of the leapfrog fluctuation's mean at this volume)
+    for x in (e64, e32):
+        assert abs(x[100:].mean() - x[:100].mean()) / x.mean() < 2e-4
+    assert abs(e32.mean() - e64.mean()) / e64.mean() < 2e-4
+    assert l32.observables().unit_max < 1e-5  # periodic FP64 reunitarisation keeps FP32 links on the group

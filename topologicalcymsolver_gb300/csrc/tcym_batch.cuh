@@ -39,19 +39,18 @@ __device__ __forceinline__ int find_member(const Member<T> *m, int n, int item, 
 // Step k of a chunk for every member: reads U[cur ^ (k&1)], writes U[cur ^ (k&1) ^ 1].
 template <int FMT>
 __global__ void __launch_bounds__(threads_for<FMT>(), min_blocks_for<FMT>())
-    k_step_batch(const Member<typename Fmt<FMT>::T> *members, int nmembers, int total_blocks, int k) {
-    using T = typename Fmt<FMT>::T;
+    k_step_batch(const Member<typename Fmt<FMT>::T> *__restrict__ members, int nmembers, int total_blocks, int k) {
     for (int item = blockIdx.x; item < total_blocks; item += gridDim.x) {
         const int mi = find_member(members, nmembers, item, false);
-        // the member into registers: stores to the fields could otherwise alias the table
-        const Geom g = members[mi].g;
-        const int64_t s = (int64_t)(item - members[mi].block_begin) * blockDim.x + threadIdx.x;
+        // the table is read-only and never aliases the fields (__restrict__), so
+        // the coefficients are read where used, block-uniform, from L1, rather
+        // than held in registers for the whole step
+        const Member<typename Fmt<FMT>::T> &m = members[mi];
+        const Geom g = m.g;
+        const int64_t s = (int64_t)(item - m.block_begin) * blockDim.x + threadIdx.x;
         if (s < g.V) {
-            StepCoef<T> c = members[mi].c;
-            c.step += (uint64_t)k;
-            const int in = members[mi].cur ^ (k & 1);
-            void *uin = members[mi].U[in], *uout = members[mi].U[in ^ 1], *e = members[mi].E;
-            site_step<Fmt<FMT>, true, true>(g, uin, uout, e, c, s);
+            const int in = m.cur ^ (k & 1);
+            site_step<Fmt<FMT>, true, true>(g, m.U[in], m.U[in ^ 1], m.E, m.c, s, (uint64_t)k);
         }
     }
 }

@@ -20,6 +20,12 @@
 #include "tcym_batch.cuh"
 #include "tcym_internal.h"
 
+// 1: the step grid is one wave of resident blocks walking the work items;
+// 0: one block per work item, scheduled by the hardware.
+#ifndef TCYM_BATCH_PERSISTENT
+#define TCYM_BATCH_PERSISTENT 1
+#endif
+
 using namespace tcym;
 
 namespace {
@@ -93,7 +99,11 @@ template <int FMT> static void fill_group(tcym_ensemble ens, FmtGroup &G, int sm
     }
     G.total_blocks = blk;
     G.red_total = red;
+#if TCYM_BATCH_PERSISTENT
     G.grid = std::max(1, std::min(blk, sm_count * LaunchBatch<FMT>::resident_blocks()));
+#else
+    G.grid = std::max(1, blk);
+#endif
     G.red_grid = std::max(1, std::min(red, sm_count * 8));
     G.h_members.resize(sizeof(Member<T>) * tab.size());
     if (!tab.empty()) std::memcpy(G.h_members.data(), tab.data(), G.h_members.size());
@@ -288,7 +298,6 @@ extern "C" int tcym_ensemble_step(tcym_ensemble ens, int nsteps) {
         if ((r = capture(ens, nsteps))) return r;
     CKE(cudaGraphLaunch(ens->exec, ens->st[0]));
     // bookkeeping of every member; periodic FP64 reunitarisation of FP32 links
-    bool reunit = false;
     for (EnsMember &m : ens->members) {
         tcym_lattice L = m.lat;
         L->cur ^= (nsteps & 1);
@@ -305,10 +314,8 @@ extern "C" int tcym_ensemble_step(tcym_ensemble ens, int nsteps) {
             }
             if (rr != cudaSuccess) return fail(ens->ctx, (cudaError_t)rr, "ensemble reunitarize");
             L->steps_since_reunit = 0;
-            reunit = true;
         }
     }
-    (void)reunit;
     CKE(cudaStreamSynchronize(ens->st[0]));
     return TCYM_OK;
 }

@@ -23,14 +23,22 @@ enum : int {
     R_NCS = 12, R_NCS_COMP = 13, R_NONFINITE = 14, R_WIDTH = 16
 };
 
-constexpr int kThreadsSU2 = 256;
+#ifndef TCYM_SU2_THREADS
+#define TCYM_SU2_THREADS 128
+#endif
+constexpr int kThreadsSU2 = TCYM_SU2_THREADS;
 constexpr int kThreadsSU3 = 128;
 constexpr int kRedThreads = 256;
-// Resident blocks per SM requested for the SU(3) step (register cap = 65536 / (blocks * threads)).
+// Resident blocks per SM requested for the step kernels (register cap = 65536 / (blocks * threads)).
 #ifndef TCYM_SU3_STEP_MINBLOCKS
-#define TCYM_SU3_STEP_MINBLOCKS 5
+#define TCYM_SU3_STEP_MINBLOCKS 4
 #endif
-template <int FMT> constexpr int min_blocks_for() { return Fmt<FMT>::NA == 3 ? 1 : TCYM_SU3_STEP_MINBLOCKS; }
+#ifndef TCYM_SU2_STEP_MINBLOCKS
+#define TCYM_SU2_STEP_MINBLOCKS 8
+#endif
+template <int FMT> constexpr int min_blocks_for() {
+    return Fmt<FMT>::NA == 8 ? TCYM_SU3_STEP_MINBLOCKS : (FMT == FMT_SU2_F32 ? TCYM_SU2_STEP_MINBLOCKS : 1);
+}
 
 template <int FMT> constexpr int threads_for() { return Fmt<FMT>::NA == 3 ? kThreadsSU2 : kThreadsSU3; }
 

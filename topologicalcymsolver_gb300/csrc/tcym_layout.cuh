@@ -27,29 +27,43 @@ struct Geom {
     int64_t V;
 };
 
-// Periodic neighbourhood of one site: wrapped coordinates x-1, x, x+1 (etc.).
-struct Nbhd {
-    int xs[3], ys[3], zs[3];
-    int nx, ny;
-    TCYM_HD Nbhd(const Geom &g, int64_t s) {
-        nx = g.nx; ny = g.ny;
-        int x = (int)(s % g.nx);
-        int64_t r = s / g.nx;
-        int y = (int)(r % g.ny);
-        int z = (int)(r / g.ny);
-        xs[0] = x == 0 ? g.nx - 1 : x - 1; xs[1] = x; xs[2] = x == g.nx - 1 ? 0 : x + 1;
-        ys[0] = y == 0 ? g.ny - 1 : y - 1; ys[1] = y; ys[2] = y == g.ny - 1 ? 0 : y + 1;
-        zs[0] = z == 0 ? g.nz - 1 : z - 1; zs[1] = z; zs[2] = z == g.nz - 1 ? 0 : z + 1;
-    }
-    // site at offset (dx,dy,dz), each in {-1,0,1}
-    TCYM_HD int64_t at(int dx, int dy, int dz) const {
-        return (int64_t)xs[dx + 1] + (int64_t)nx * ((int64_t)ys[dy + 1] + (int64_t)ny * zs[dz + 1]);
-    }
-    TCYM_HD int64_t off(const int *d) const { return at(d[0], d[1], d[2]); }
-    TCYM_HD int parity() const { return (xs[1] + ys[1] + zs[1]) & 1; }
-};
+// a[i] for a direction i known only at run time, by selects: indexing a small
+// array with a run-time index would place it in local memory.
+template <class T> TCYM_HD T sel3(const T (&a)[3], int i) { return i == 0 ? a[0] : (i == 1 ? a[1] : a[2]); }
 
-TCYM_HD void unit(int mu, int *d) { d[0] = mu == 0; d[1] = mu == 1; d[2] = mu == 2; }
+// Periodic neighbourhood of one site: the signed site-index offsets of its
+// forward and backward neighbour along each axis (the wrap folded in), so a
+// neighbour of a run-time direction is s + a select, all in registers.
+// Extents stay below 2^31 sites per plane, so offsets fit 32 bits.
+struct Nbhd {
+    int64_t s;
+    int fx, fy, fz, bx, by, bz;
+    int par;
+    TCYM_HD Nbhd(const Geom &g, int64_t site) : s(site) {
+        const int x = (int)(site % g.nx);
+        const int64_t r = site / g.nx;
+        const int y = (int)(r % g.ny);
+        const int z = (int)(r / g.ny);
+        const int sy = g.nx, sz = g.nx * g.ny;
+        fx = x == g.nx - 1 ? 1 - g.nx : 1;
+        bx = x == 0 ? g.nx - 1 : -1;
+        fy = y == g.ny - 1 ? (1 - g.ny) * sy : sy;
+        by = y == 0 ? (g.ny - 1) * sy : -sy;
+        fz = z == g.nz - 1 ? (1 - g.nz) * sz : sz;
+        bz = z == 0 ? (g.nz - 1) * sz : -sz;
+        par = (x + y + z) & 1;
+    }
+    // offset of one step along axis d, a in {-1, 0, 1} (a is a constant at every call site)
+    TCYM_HD int step(int d, int a) const {
+        if (a == 0) return 0;
+        return a > 0 ? (d == 0 ? fx : (d == 1 ? fy : fz)) : (d == 0 ? bx : (d == 1 ? by : bz));
+    }
+    // the site s + a e_d
+    TCYM_HD int64_t at(int d, int a) const { return s + step(d, a); }
+    // the site s + a e_mu + b e_nu, mu != nu
+    TCYM_HD int64_t at(int mu, int a, int nu, int b) const { return s + step(mu, a) + step(nu, b); }
+    TCYM_HD int parity() const { return par; }
+};
 
 enum Format : int { FMT_SU2_F32 = 0, FMT_SU2_F64 = 1, FMT_SU3_F32 = 2, FMT_SU3_F64 = 3 };
 

@@ -36,29 +36,25 @@ template <class T> struct StepCoef {
 // bracket [c_nu1 (P_{mu nu1} - P_{mu,-nu1}) - c_nu2 (P_{nu2 mu} - P_{-nu2,mu})]
 // (Dynamics.cpp:184-188) equals proj(U_mu A).
 template <class F>
-TCYM_HD typename F::Mat staple_sum(const void *U, int64_t V, const Nbhd &nb, int mu, const typename F::T *cnu) {
+TCYM_HD typename F::Mat staple_sum(const void *U, int64_t V, const Nbhd &nb, int mu,
+                                  const typename F::T (&cnu)[3]) {
     using G = typename F::G;
     using M = typename F::Mat;
-    int dm[3];
-    unit(mu, dm);
     M A = G::zero();
 #pragma unroll
     for (int k = 1; k <= 2; ++k) {
-        const int nu = (mu + k) % 3;
-        int dn[3];
-        unit(nu, dn);
-        const int pm[3] = {dm[0] - dn[0], dm[1] - dn[1], dm[2] - dn[2]};
-        const int mn[3] = {-dn[0], -dn[1], -dn[2]};
+        const int nu = mu + k >= 3 ? mu + k - 3 : mu + k;
         // staples are group elements: mulu forms rows 0 and 1 and rebuilds row 2
-        M a1 = F::load(U, V, nu, nb.off(dm));
-        M a2 = F::load(U, V, mu, nb.off(dn));
-        M a3 = F::load(U, V, nu, nb.at(0, 0, 0));
+        M a1 = F::load(U, V, nu, nb.at(mu, 1));
+        M a2 = F::load(U, V, mu, nb.at(nu, 1));
+        M a3 = F::load(U, V, nu, nb.s);
         M up = G::template mulu<false, true>(G::template mulu<false, true>(a1, a2), a3);
-        M b1 = F::load(U, V, nu, nb.off(pm));
-        M b2 = F::load(U, V, mu, nb.off(mn));
-        M b3 = F::load(U, V, nu, nb.off(mn));
+        M b1 = F::load(U, V, nu, nb.at(mu, 1, nu, -1));
+        const int64_t sb = nb.at(nu, -1);
+        M b2 = F::load(U, V, mu, sb);
+        M b3 = F::load(U, V, nu, sb);
         M lo = G::template mulu<false, false>(G::template mulu<true, true>(b1, b2), b3);
-        A = G::add(A, G::scale(cnu[nu], G::add(up, lo)));
+        A = G::add(A, G::scale(sel3(cnu, nu), G::add(up, lo)));
     }
     return A;
 }
@@ -68,7 +64,7 @@ TCYM_HD typename F::Mat staple_sum(const void *U, int64_t V, const Nbhd &nb, int
 // DO_E is false, i.e. for the pointwise link update).
 template <class F, bool DO_E, bool DO_U>
 TCYM_HD void site_step(const Geom &g, const void *Uin, void *Uout, void *E, const StepCoef<typename F::T> &c,
-                       int64_t s) {
+                       int64_t s, uint64_t step_add = 0) {
     using G = typename F::G;
     using T = typename F::T;
     using M = typename F::Mat;
@@ -84,22 +80,24 @@ TCYM_HD void site_step(const Geom &g, const void *Uin, void *Uout, void *E, cons
             M A = staple_sum<F>(Uin, V, nb, mu, c.cnu);
             T f[NA];
             G::proj_mul(u, A, f);
+            const T fc = sel3(c.fc, mu);
             if (c.mode == MODE_LANGEVIN) {
                 T xi[NA];
-                normals<T, NA>(c.seed, STREAM_NOISE, c.step, (uint32_t)s, (uint32_t)mu, xi);
+                normals<T, NA>(c.seed, STREAM_NOISE, c.step + step_add, (uint32_t)s, (uint32_t)mu, xi);
+                const T damp = sel3(c.damp, mu), kick = sel3(c.kick, mu);
 #pragma unroll
-                for (int a = 0; a < NA; ++a) e[a] = e[a] + (c.fc[mu] * f[a] - c.damp[mu] * e[a] + c.kick[mu] * xi[a]);
+                for (int a = 0; a < NA; ++a) e[a] = e[a] + (fc * f[a] - damp * e[a] + kick * xi[a]);
             } else if (c.mode == MODE_FLOW) {
 #pragma unroll
-                for (int a = 0; a < NA; ++a) e[a] = c.fc[mu] * f[a];
+                for (int a = 0; a < NA; ++a) e[a] = fc * f[a];
             } else {
 #pragma unroll
-                for (int a = 0; a < NA; ++a) e[a] = e[a] + c.fc[mu] * f[a];
+                for (int a = 0; a < NA; ++a) e[a] = e[a] + fc * f[a];
             }
             F::store_e(E, V, mu, s, e);
         }
         if (DO_U) {
-            F::store(Uout, V, mu, s, G::iexp_mul(c.uc[mu], e, u));
+            F::store(Uout, V, mu, s, G::iexp_mul(sel3(c.uc, mu), e, u));
         }
     }
 }
@@ -108,8 +106,8 @@ TCYM_HD void site_step(const Geom &g, const void *Uin, void *Uout, void *E, cons
 // exp(-i dtau F_mu(x)), F = fc proj(U_mu A) (no reference counterpart; the
 // reference flows all links at once, GradientFlow.cpp:150-165).
 template <class F>
-TCYM_HD void link_flow(const Geom &g, void *U, int mu, const typename F::T *fc, const typename F::T *cnu,
-                       const typename F::T *uc, int64_t s) {
+TCYM_HD void link_flow(const Geom &g, void *U, int mu, const typename F::T (&fc)[3], const typename F::T (&cnu)[3],
+                       const typename F::T (&uc)[3], int64_t s) {
     using G = typename F::G;
     using T = typename F::T;
     using M = typename F::Mat;
@@ -118,9 +116,10 @@ TCYM_HD void link_flow(const Geom &g, void *U, int mu, const typename F::T *fc, 
     M u = F::load(U, g.V, mu, s);
     T f[F::NA];
     G::proj_mul(u, A, f);
+    const T fm = sel3(fc, mu);
 #pragma unroll
-    for (int a = 0; a < F::NA; ++a) f[a] *= fc[mu];
-    F::store(U, g.V, mu, s, G::iexp_mul(uc[mu], f, u));
+    for (int a = 0; a < F::NA; ++a) f[a] *= fm;
+    F::store(U, g.V, mu, s, G::iexp_mul(sel3(uc, mu), f, u));
 }
 
 // ----------------------------------------------------------------- observables
@@ -131,31 +130,28 @@ template <class F>
 TCYM_HD void clover_leaves(const void *U, int64_t V, const Nbhd &nb, int mu, int nu, typename F::Mat *Q) {
     using G = typename F::G;
     using M = typename F::Mat;
-    int dm[3], dn[3];
-    unit(mu, dm);
-    unit(nu, dn);
-    const int o[3] = {0, 0, 0};
-    auto L = [&](int d, int x, int y, int z) { int t[3] = {x, y, z}; return F::load(U, V, d, nb.off(t)); };
+    // link along d at x + a e_mu + b e_nu
+    auto L = [&](int d, int a, int b) { return F::load(U, V, d, nb.at(mu, a, nu, b)); };
     // Q0 = U_mu(x) U_nu(x+mu) U_mu^dag(x+nu) U_nu^dag(x)
-    M a = L(mu, o[0], o[1], o[2]), b = L(nu, dm[0], dm[1], dm[2]), c = L(mu, dn[0], dn[1], dn[2]), d = L(nu, 0, 0, 0);
+    M a = L(mu, 0, 0), b = L(nu, 1, 0), c = L(mu, 0, 1), d = L(nu, 0, 0);
     Q[0] = G::mul(G::mul(a, b), G::template mulx<true, true>(c, d));
     // Q1 = U_nu(x) U_mu^dag(x+nu-mu) U_nu^dag(x-mu) U_mu(x-mu)
-    a = L(nu, 0, 0, 0);
-    b = L(mu, dn[0] - dm[0], dn[1] - dm[1], dn[2] - dm[2]);
-    c = L(nu, -dm[0], -dm[1], -dm[2]);
-    d = L(mu, -dm[0], -dm[1], -dm[2]);
+    a = L(nu, 0, 0);
+    b = L(mu, -1, 1);
+    c = L(nu, -1, 0);
+    d = L(mu, -1, 0);
     Q[1] = G::mul(G::template mulx<false, true>(a, b), G::template mulx<true, false>(c, d));
     // Q2 = U_nu^dag(x-nu) U_mu(x-nu) U_nu(x-nu+mu) U_mu^dag(x)
-    a = L(nu, -dn[0], -dn[1], -dn[2]);
-    b = L(mu, -dn[0], -dn[1], -dn[2]);
-    c = L(nu, dm[0] - dn[0], dm[1] - dn[1], dm[2] - dn[2]);
-    d = L(mu, 0, 0, 0);
+    a = L(nu, 0, -1);
+    b = L(mu, 0, -1);
+    c = L(nu, 1, -1);
+    d = L(mu, 0, 0);
     Q[2] = G::mul(G::template mulx<true, false>(a, b), G::template mulx<false, true>(c, d));
     // Q3 = U_mu^dag(x-mu) U_nu^dag(x-mu-nu) U_mu(x-mu-nu) U_nu(x-nu)
-    a = L(mu, -dm[0], -dm[1], -dm[2]);
-    b = L(nu, -dm[0] - dn[0], -dm[1] - dn[1], -dm[2] - dn[2]);
-    c = L(mu, -dm[0] - dn[0], -dm[1] - dn[1], -dm[2] - dn[2]);
-    d = L(nu, -dn[0], -dn[1], -dn[2]);
+    a = L(mu, -1, 0);
+    b = L(nu, -1, -1);
+    c = L(mu, -1, -1);
+    d = L(nu, 0, -1);
     Q[3] = G::mul(G::template mulx<true, true>(a, b), G::mul(c, d));
 }
 
@@ -222,11 +218,10 @@ template <class F> TCYM_HD double site_edotb_improved(const Geom &g, const void 
         M avg = G::add(G::scale(T(5.0 / 12.0), boxes), G::scale(T(-1.0 / 24.0), rects));
         T b[NA];
         G::proj(avg, b);
-        int d[3];
-        unit(i, d);
-        const int64_t sp = site_offset(g, x, y, z, d[0], d[1], d[2]);
-        const int64_t sm = site_offset(g, x, y, z, -d[0], -d[1], -d[2]);
-        const int64_t sm2 = site_offset(g, x, y, z, -2 * d[0], -2 * d[1], -2 * d[2]);
+        const int dx = i == 0, dy = i == 1, dz = i == 2;
+        const int64_t sp = site_offset(g, x, y, z, dx, dy, dz);
+        const int64_t sm = site_offset(g, x, y, z, -dx, -dy, -dz);
+        const int64_t sm2 = site_offset(g, x, y, z, -2 * dx, -2 * dy, -2 * dz);
         T e0[NA], ep[NA], em[NA], em2[NA], t1[NA], t2[NA], t3[NA];
         F::load_e(E, g.V, i, s, e0);
         F::load_e(E, g.V, i, sp, ep);
@@ -275,16 +270,15 @@ TCYM_HD void site_observables(const Geom &g, const void *U, const void *E, int m
     }
     T et[3][NA];  // U_mu^dag(x-mu) E_mu(x-mu) U_mu(x-mu): shared by Gauss and clover E
     if (mask & (OBS_GAUSS | OBS_EDOTB)) {
+#pragma unroll
         for (int mu = 0; mu < 3; ++mu) {
-            int d[3];
-            unit(mu, d);
-            const int m[3] = {-d[0], -d[1], -d[2]};
-            int64_t sm = nb.off(m);
+            const int64_t sm = nb.at(mu, -1);
             T e[NA];
             F::load_e(E, V, mu, sm, e);
             G::inverse_adjoint(F::load(U, V, mu, sm), e, et[mu]);
         }
     }
+#pragma unroll
     for (int mu = 0; mu < 3; ++mu) {
         T e[NA];
         F::load_e(E, V, mu, s, e);
@@ -301,10 +295,7 @@ TCYM_HD void site_observables(const Geom &g, const void *U, const void *E, int m
             if (mask & OBS_EDOTB) {
                 clover_leaves<F>(U, V, nb, j, k, Q);
             } else {
-                int dj[3], dk[3];
-                unit(j, dj);
-                unit(k, dk);
-                M a = F::load(U, V, j, s), b = F::load(U, V, k, nb.off(dj)), c = F::load(U, V, j, nb.off(dk)),
+                M a = F::load(U, V, j, s), b = F::load(U, V, k, nb.at(j, 1)), c = F::load(U, V, j, nb.at(k, 1)),
                   d = F::load(U, V, k, s);
                 Q[0] = G::mul(G::mul(a, b), G::template mulx<true, true>(c, d));
             }
@@ -329,11 +320,9 @@ TCYM_HD void site_gauss(const Geom &g, const void *U, const void *E, int64_t s, 
     constexpr int NA = F::NA;
     Nbhd nb(g, s);
     for (int a = 0; a < NA; ++a) gv[a] = 0;
+#pragma unroll
     for (int mu = 0; mu < 3; ++mu) {
-        int d[3];
-        unit(mu, d);
-        const int m[3] = {-d[0], -d[1], -d[2]};
-        int64_t sm = nb.off(m);
+        const int64_t sm = nb.at(mu, -1);
         T e[NA], em[NA], t[NA];
         F::load_e(E, g.V, mu, s, e);
         F::load_e(E, g.V, mu, sm, em);
@@ -350,10 +339,9 @@ TCYM_HD void site_gauss_update(const Geom &g, const void *U, void *E, const doub
     using T = typename F::T;
     constexpr int NA = F::NA;
     Nbhd nb(g, s);
+#pragma unroll
     for (int mu = 0; mu < 3; ++mu) {
-        int d[3];
-        unit(mu, d);
-        int64_t sp = nb.off(d);
+        const int64_t sp = nb.at(mu, 1);
         T gp[NA], t[NA], e[NA];
         for (int a = 0; a < NA; ++a) gp[a] = (T)Gs[a * g.V + sp];
         G::adjoint(F::load(U, g.V, mu, s), gp, t);
