@@ -20,10 +20,12 @@
 #include "tcym_batch.cuh"
 #include "tcym_internal.h"
 
-// 1: the step grid is one wave of resident blocks walking the work items;
-// 0: one block per work item, scheduled by the hardware.
+// 0 (default): one block per work item, scheduled by the hardware, so the
+// formats' launches interleave on the SMs and tails fill; 1: one wave of
+// resident blocks walking the work items (measured 6% slower on a 256-member
+// mixed ensemble).
 #ifndef TCYM_BATCH_PERSISTENT
-#define TCYM_BATCH_PERSISTENT 1
+#define TCYM_BATCH_PERSISTENT 0
 #endif
 
 using namespace tcym;
