@@ -27,7 +27,8 @@ def load():
         L.hc_from_aos.argtypes = [ctypes.c_int, ip, _vp, _vp, _vp, _vp]
         L.hc_to_aos.argtypes = [ctypes.c_int, ip, _vp, _vp, _vp, _vp]
         L.hc_step.argtypes = [ctypes.c_int, ip, _vp, _vp, _vp, ctypes.c_int, ctypes.c_double, ctypes.c_double,
-                              ctypes.c_double, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int, ctypes.c_int]
+                              ctypes.c_double, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int, ctypes.c_int,
+                              ctypes.c_int]
         L.hc_flow_cb.argtypes = [ctypes.c_int, ip, _vp, ctypes.c_double, ctypes.c_int]
         L.hc_observables.argtypes = [ctypes.c_int, ip, _vp, _vp, ctypes.c_int, _vp]
         L.hc_gauss_restore.argtypes = [ctypes.c_int, ip, _vp, _vp, ctypes.c_double, ctypes.c_int]
@@ -54,9 +55,12 @@ class HostLattice:
         self.shape = tuple(shape)
         self.n = (ctypes.c_int * 3)(*shape)
         self.V = int(np.prod(shape))
-        self.U = [np.zeros(3 * LINK_BYTES[self.fmt] * self.V, np.uint8) for _ in range(2)]
-        self.E = np.zeros(3 * FIELD_BYTES[self.fmt] * self.V, np.uint8)
+        # the FP32 formats store site pairs, padded to an even site count
+        stored = 2 * ((self.V + 1) // 2) if prec == "f32" else self.V
+        self.U = [np.zeros(3 * LINK_BYTES[self.fmt] * stored, np.uint8) for _ in range(2)]
+        self.E = np.zeros(3 * FIELD_BYTES[self.fmt] * stored, np.uint8)
         self.cur = 0
+        self.pairs = 1  # 0: force the per-site step
 
     def upload(self, U=None, E=None):
         self.L.hc_from_aos(self.fmt, self.n, None if U is None else _p(U), None if E is None else _p(E),
@@ -71,11 +75,11 @@ class HostLattice:
     def step(self, mode, dt, gamma=0.0, T=0.0, seed=0, step=0, do_e=True, do_u=True):
         if do_e and do_u:
             self.L.hc_step(self.fmt, self.n, _p(self.U[self.cur]), _p(self.U[1 - self.cur]), _p(self.E), mode, dt,
-                           gamma, T, seed, step, 1, 1)
+                           gamma, T, seed, step, 1, 1, self.pairs)
             self.cur ^= 1
         else:
             self.L.hc_step(self.fmt, self.n, _p(self.U[self.cur]), _p(self.U[self.cur]), _p(self.E), mode, dt, gamma,
-                           T, seed, step, int(do_e), int(do_u))
+                           T, seed, step, int(do_e), int(do_u), self.pairs)
 
     def leapfrog(self, dt, nsteps):
         for _ in range(nsteps):

@@ -86,6 +86,30 @@ def test_site_step_leapfrog_langevin_flow(oracle_port, nc, prec):
     assert rel(Uh, U) < TOL[prec] and rel(Eh, E) < TOL[prec]
 
 
+@pytest.mark.parametrize("nc", [2, 3])
+@pytest.mark.parametrize("shape", [(8, 8, 16), (6, 4, 2), (5, 5, 5)])
+def test_site_pair_step(oracle_port, nc, shape):
+    """The FP32 formats' paired step against the oracle and against the per-site
+    step on the same paired layout: (8,8,16) has seam and interior blocks of
+    128 pairs; at nz = 2 a pair's partner is its own z-neighbour; odd V (5^3)
+    has a padding site and no paired step."""
+    P = oracle_port[nc]
+    U, E = _state(P, nc, shape, 21)
+    H = hc.HostLattice(nc, "f32", shape)
+    S = hc.HostLattice(nc, "f32", shape)
+    S.pairs = 0
+    for X in (H, S):
+        X.upload(U, E)
+        X.leapfrog(0.05, 5)
+        X.langevin(0.02, 1.0, 0.6, 7, 0, 3)
+    P.leapfrog(shape, U, E, 0.05, 5)
+    P.langevin(shape, U, E, 0.02, 1.0, 0.6, 7, 0, 3)
+    Uh, Eh = H.download()
+    Us, Es = S.download()
+    assert rel(Uh, U) < 1e-5 and rel(Eh, E) < 1e-5
+    assert rel(Uh, Us) < 1e-5 and rel(Eh, Es) < 1e-5
+
+
 @pytest.mark.parametrize("nc,prec", FORMATS)
 def test_site_checkerboard_flow(oracle_port, nc, prec):
     P = oracle_port[nc]

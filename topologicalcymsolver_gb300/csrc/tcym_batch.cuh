@@ -1,9 +1,10 @@
 // Batched kernels: many independent lattices of one storage format advance in
-// one launch.  A persistent grid walks a flattened list of (member, block)
-// work items; each work item is exactly the block the single-lattice kernel
-// would run, calling the same per-site function with the member's own
-// geometry, buffers and coefficients, so a member's arithmetic does not depend
-// on which other lattices share the launch.
+// one launch.  The grid walks a flattened list of (member, block) work items;
+// each work item is exactly the block the single-lattice kernel would run
+// (site pairs for FP32 members with even nz, single sites otherwise), calling
+// the same per-site function with the member's own geometry, buffers and
+// coefficients, so a member's arithmetic does not depend on which other
+// lattices share the launch.
 #pragma once
 
 #include "tcym_kernels.cuh"
@@ -21,8 +22,13 @@ template <class T> struct Member {
     int block_begin;     // first step work item of this member
     int red_begin;       // first reduction work item of this member
     int red_blocks;      // reduction work items of this member
+    int paired;          // step work items cover site pairs (FP32 format, even nz)
     double ncs_dt;       // Kahan increment factor for measurements (0: no N_CS update)
 };
+
+template <int FMT> constexpr int batch_min_blocks_for() {
+    return Fmt<FMT>::PAIRED ? pair_min_blocks_for<FMT>() : min_blocks_for<FMT>();
+}
 
 // index of the member owning work item `item` (begins sorted ascending)
 template <class T>
@@ -38,8 +44,9 @@ __device__ __forceinline__ int find_member(const Member<T> *m, int n, int item, 
 
 // Step k of a chunk for every member: reads U[cur ^ (k&1)], writes U[cur ^ (k&1) ^ 1].
 template <int FMT>
-__global__ void __launch_bounds__(threads_for<FMT>(), min_blocks_for<FMT>())
+__global__ void __launch_bounds__(threads_for<FMT>(), batch_min_blocks_for<FMT>())
     k_step_batch(const Member<typename Fmt<FMT>::T> *__restrict__ members, int nmembers, int total_blocks, int k) {
+    static_assert(!Fmt<FMT>::PAIRED || threads_for<FMT>() == kThreadsPair, "one block shape for both paths");
     for (int item = blockIdx.x; item < total_blocks; item += gridDim.x) {
         const int mi = find_member(members, nmembers, item, false);
         // the table is read-only and never aliases the fields (__restrict__), so
@@ -47,6 +54,19 @@ __global__ void __launch_bounds__(threads_for<FMT>(), min_blocks_for<FMT>())
         // than held in registers for the whole step
         const Member<typename Fmt<FMT>::T> &m = members[mi];
         const Geom g = m.g;
+        if constexpr (Fmt<FMT>::PAIRED) {
+            if (m.paired) {  // block-uniform
+                const int64_t p0 = (int64_t)(item - m.block_begin) * blockDim.x, p = p0 + threadIdx.x;
+                if (p < (g.V >> 1)) {
+                    const int in = m.cur ^ (k & 1);
+                    if (pairs_touch_seam(g, p0, blockDim.x))
+                        site_step_pair<Fmt<FMT>, true>(g, m.U[in], m.U[in ^ 1], m.E, m.c, p, (uint64_t)k);
+                    else
+                        site_step_pair<Fmt<FMT>, false>(g, m.U[in], m.U[in ^ 1], m.E, m.c, p, (uint64_t)k);
+                }
+                continue;
+            }
+        }
         const int64_t s = (int64_t)(item - m.block_begin) * blockDim.x + threadIdx.x;
         if (s < g.V) {
             const int in = m.cur ^ (k & 1);

@@ -64,6 +64,10 @@ size_t tcym_link_bytes(int fmt) {
         default: return 144;
     }
 }
+// sites stored per plane: the FP32 formats hold site pairs, padded to even V
+size_t tcym_stored_sites(int fmt, int64_t V) {
+    return (fmt == FMT_SU2_F32 || fmt == FMT_SU3_F32) ? 2 * (size_t)pair_sites(V) : (size_t)V;
+}
 size_t tcym_field_bytes(int fmt) {
     switch (fmt) {
         case FMT_SU2_F32: return 12;
@@ -177,7 +181,8 @@ extern "C" int tcym_lattice_create_ex(tcym_ctx ctx, int nc, int nx, int ny, int 
     };
     cudaError_t e;
     if ((e = cudaStreamCreateWithFlags(&lat->stream, cudaStreamNonBlocking)) != cudaSuccess) return fail(e, "stream");
-    const size_t ub = 3 * tcym_link_bytes(lat->fmt) * (size_t)V, eb = 3 * tcym_field_bytes(lat->fmt) * (size_t)V;
+    const size_t nst = tcym_stored_sites(lat->fmt, V);
+    const size_t ub = 3 * tcym_link_bytes(lat->fmt) * nst, eb = 3 * tcym_field_bytes(lat->fmt) * nst;
     if ((e = cudaMalloc(&lat->U[0], ub)) != cudaSuccess) return fail(e, "cudaMalloc(U)");
     if ((e = cudaMalloc(&lat->U[1], ub)) != cudaSuccess) return fail(e, "cudaMalloc(U')");
     if ((e = cudaMalloc(&lat->E, eb)) != cudaSuccess) return fail(e, "cudaMalloc(E)");
@@ -268,8 +273,8 @@ extern "C" int tcym_lattice_copy(tcym_lattice dst, const tcym_lattice src) {
     cudaSetDevice(ctx->device);
     CK(cudaStreamSynchronize(src->stream));
     if (dst->fmt == src->fmt) {
-        const size_t ub = 3 * tcym_link_bytes(dst->fmt) * (size_t)dst->g.V;
-        const size_t eb = 3 * tcym_field_bytes(dst->fmt) * (size_t)dst->g.V;
+        const size_t nst = tcym_stored_sites(dst->fmt, dst->g.V);
+        const size_t ub = 3 * tcym_link_bytes(dst->fmt) * nst, eb = 3 * tcym_field_bytes(dst->fmt) * nst;
         CK(cudaMemcpyAsync(dst->U[dst->cur], src->U[src->cur], ub, cudaMemcpyDeviceToDevice, dst->stream));
         CK(cudaMemcpyAsync(dst->E, src->E, eb, cudaMemcpyDeviceToDevice, dst->stream));
     } else {

@@ -93,7 +93,8 @@ template <int FMT> static void fill_group(tcym_ensemble ens, FmtGroup &G, int sm
         m.c = coef_cast<T>(tcym_coef(L->a, em.mode, em.dt, em.gamma, em.T, em.seed, em.next_step));
         m.cur = L->cur;
         m.block_begin = blk;
-        blk += grid_for(L->g.V, TPB);
+        m.paired = Fmt<FMT>::PAIRED && L->g.nz % 2 == 0;
+        blk += grid_for(m.paired ? L->g.V / 2 : L->g.V, TPB);
         m.red_begin = red;
         m.red_blocks = grid_for(L->g.V, kRedThreads);
         red += m.red_blocks;

@@ -48,8 +48,22 @@ template <int FMT> struct H {
     using F = Fmt<FMT>;
     using T = typename F::T;
     static void step(const Geom &g, const void *Uin, void *Uout, void *E, const StepCoef<double> &cd, int doE,
-                     int doU) {
+                     int doU, int pairs) {
         StepCoef<T> c = cast<T>(cd);
+        if constexpr (F::PAIRED) {
+            // the device's paired step, block by block as the kernel runs it (128 pairs a block)
+            if (pairs && doE && doU && g.nz % 2 == 0) {
+                const int64_t Vh = g.V / 2;
+                for (int64_t p0 = 0; p0 < Vh; p0 += 128) {
+                    const bool seam = pairs_touch_seam(g, p0, 128);
+                    for (int64_t p = p0; p < p0 + 128 && p < Vh; ++p) {
+                        if (seam) site_step_pair<F, true>(g, Uin, Uout, E, c, p);
+                        else site_step_pair<F, false>(g, Uin, Uout, E, c, p);
+                    }
+                }
+                return;
+            }
+        }
         for (int64_t s = 0; s < g.V; ++s) {
             if (doE && doU) site_step<F, true, true>(g, Uin, Uout, E, c, s);
             else if (doE) site_step<F, true, false>(g, Uin, Uout, E, c, s);
@@ -152,11 +166,12 @@ int hc_to_aos(int fmt, const int *n, const void *U, const void *E, double *Ua, d
     HC_DISPATCH(fmt, for (int64_t s = 0; s < g.V; ++s) site_to_aos<HH::F>(g, U, E, Ua, Ea, s));
     return 0;
 }
+// pairs: take the paired step where the device does (FP32 formats, even nz, fused step)
 int hc_step(int fmt, const int *n, const void *Uin, void *Uout, void *E, int mode, double dt, double gamma, double T,
-            uint64_t seed, uint64_t step, int doE, int doU) {
+            uint64_t seed, uint64_t step, int doE, int doU, int pairs) {
     Geom g = geom(n);
     StepCoef<double> c = coef(mode, dt, gamma, T, seed, step);
-    HC_DISPATCH(fmt, HH::step(g, Uin, Uout, E, c, doE, doU));
+    HC_DISPATCH(fmt, HH::step(g, Uin, Uout, E, c, doE, doU, pairs));
     return 0;
 }
 int hc_flow_cb(int fmt, const int *n, void *U, double dtau, int nsweeps) {

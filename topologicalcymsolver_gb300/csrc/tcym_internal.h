@@ -42,6 +42,7 @@ void tcym_set_error(tcym_ctx ctx, const char *fmt, ...);
 int tcym_format_of(int nc, int precision);
 size_t tcym_link_bytes(int fmt);
 size_t tcym_field_bytes(int fmt);
+size_t tcym_stored_sites(int fmt, int64_t V);
 tcym::StepCoef<double> tcym_coef(const double *a, int mode, double dt, double gamma, double T, uint64_t seed,
                                  uint64_t step);
 int tcym_reduce(tcym_lattice lat, int mask, double ncs_dt);

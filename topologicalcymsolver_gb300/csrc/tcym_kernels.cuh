@@ -42,6 +42,19 @@ template <int FMT> constexpr int min_blocks_for() {
 
 template <int FMT> constexpr int threads_for() { return Fmt<FMT>::NA == 3 ? kThreadsSU2 : kThreadsSU3; }
 
+// The paired step (FP32 formats, even nz): one thread per site pair, 128 per
+// block; resident blocks per SM requested (register cap 65536 / (blocks * 128)).
+constexpr int kThreadsPair = 128;
+#ifndef TCYM_SU3_PAIR_MINBLOCKS
+#define TCYM_SU3_PAIR_MINBLOCKS 2
+#endif
+#ifndef TCYM_SU2_PAIR_MINBLOCKS
+#define TCYM_SU2_PAIR_MINBLOCKS 4
+#endif
+template <int FMT> constexpr int pair_min_blocks_for() {
+    return Fmt<FMT>::NA == 8 ? TCYM_SU3_PAIR_MINBLOCKS : TCYM_SU2_PAIR_MINBLOCKS;
+}
+
 inline int grid_for(int64_t n, int threads) {
     int64_t b = (n + threads - 1) / threads;
     return (int)(b < 1 ? 1 : b);
@@ -66,6 +79,17 @@ __global__ void __launch_bounds__(threads_for<FMT>(), min_blocks_for<FMT>()) k_s
     int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= g.V) return;
     site_step<Fmt<FMT>, DO_E, DO_U>(g, Uin, Uout, E, c, s);
+}
+
+// one thread per site pair (FP32 formats, even nz); blocks touching the seam
+// take the lane-swapping loads
+template <int FMT>
+__global__ void __launch_bounds__(kThreadsPair, pair_min_blocks_for<FMT>())
+    k_step_pair(Geom g, const void *Uin, void *Uout, void *E, StepCoef<float> c) {
+    const int64_t p0 = (int64_t)blockIdx.x * blockDim.x, p = p0 + threadIdx.x;
+    if (p >= (g.V >> 1)) return;
+    if (pairs_touch_seam(g, p0, blockDim.x)) site_step_pair<Fmt<FMT>, true>(g, Uin, Uout, E, c, p);
+    else site_step_pair<Fmt<FMT>, false>(g, Uin, Uout, E, c, p);
 }
 
 // sites of parity p, for even extents: t -> (x, row) with x of the right parity
@@ -205,6 +229,12 @@ template <int FMT> struct Launch {
     static cudaError_t step(const Geom &g, const void *Uin, void *Uout, void *E, const StepCoef<double> &cd, bool doE,
                             bool doU, cudaStream_t st) {
         StepCoef<T> c = coef_cast<T>(cd);
+        if constexpr (F::PAIRED) {
+            if (doE && doU && g.nz % 2 == 0) {
+                k_step_pair<FMT><<<grid_for(g.V >> 1, kThreadsPair), kThreadsPair, 0, st>>>(g, Uin, Uout, E, c);
+                return cudaGetLastError();
+            }
+        }
         int grid = grid_for(g.V, TPB);
         if (doE && doU) k_step<FMT, true, true><<<grid, TPB, 0, st>>>(g, Uin, Uout, E, c);
         else if (doE) k_step<FMT, true, false><<<grid, TPB, 0, st>>>(g, Uin, Uout, E, c);

@@ -76,6 +76,76 @@ template <> struct Real<double> {
     }
 };
 
+// -------------------------------------------------------------- packed pairs
+// f2: two FP32 values, one for each site of a site pair.  Every operation is
+// one packed instruction on sm_100 and later (FADD2 / FMUL2 / FFMA2), each
+// lane rounded exactly as the scalar operation; host code (and device code
+// for older targets) does the lanes one at a time.  Packing halves the
+// instructions issued for the FP32 arithmetic, which otherwise take every
+// issue slot the FP32 pipe can use.
+struct f2 {
+    float2 v;
+    f2() = default;
+    TCYM_HD explicit f2(double a) : v(make_float2((float)a, (float)a)) {}
+    TCYM_HD f2(float a, float b) : v(make_float2(a, b)) {}
+};
+TCYM_HD f2 f2_of(float2 x) { f2 r; r.v = x; return r; }
+TCYM_HD f2 operator-(f2 a) { return f2(-a.v.x, -a.v.y); }
+#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 1000
+#define TCYM_PACKED_FP32 1
+#else
+#define TCYM_PACKED_FP32 0
+#endif
+#if TCYM_PACKED_FP32
+TCYM_HD f2 operator+(f2 a, f2 b) { return f2_of(__fadd2_rn(a.v, b.v)); }
+TCYM_HD f2 operator-(f2 a, f2 b) { return f2_of(__fadd2_rn(a.v, make_float2(-b.v.x, -b.v.y))); }
+TCYM_HD f2 operator*(f2 a, f2 b) { return f2_of(__fmul2_rn(a.v, b.v)); }
+#else
+TCYM_HD f2 operator+(f2 a, f2 b) { return f2(a.v.x + b.v.x, a.v.y + b.v.y); }
+TCYM_HD f2 operator-(f2 a, f2 b) { return f2(a.v.x - b.v.x, a.v.y - b.v.y); }
+TCYM_HD f2 operator*(f2 a, f2 b) { return f2(a.v.x * b.v.x, a.v.y * b.v.y); }
+#endif
+TCYM_HD f2 &operator+=(f2 &a, f2 b) { return a = a + b; }
+TCYM_HD f2 &operator-=(f2 &a, f2 b) { return a = a - b; }
+TCYM_HD f2 &operator*=(f2 &a, f2 b) { return a = a * b; }
+using ::fma;
+TCYM_HD f2 fma(f2 a, f2 b, f2 c) {
+#if TCYM_PACKED_FP32
+    return f2_of(__ffma2_rn(a.v, b.v, c.v));
+#else
+    return f2(fmaf(a.v.x, b.v.x, c.v.x), fmaf(a.v.y, b.v.y, c.v.y));
+#endif
+}
+TCYM_HD float lane(f2 a, int l) { return l ? a.v.y : a.v.x; }
+TCYM_HD f2 lane_swap(f2 a) { return f2(a.v.y, a.v.x); }
+template <class T> struct Packed { static constexpr bool value = false; };
+template <> struct Packed<f2> { static constexpr bool value = true; };
+// a > t in any lane
+TCYM_HD bool any_gt(float a, float t) { return a > t; }
+TCYM_HD bool any_gt(double a, double t) { return a > t; }
+TCYM_HD bool any_gt(f2 a, f2 t) { return a.v.x > t.v.x || a.v.y > t.v.y; }
+
+// f = sin(d/2) / d (any finite value at d = 0, where it multiplies zeros) and
+// co = cos(d/2), d = sqrt(d2): the SU(2) exponential's coefficients.
+TCYM_HD void half_angle(float d2, float &f, float &co) {
+    if (d2 == 0.0f) { f = 0.5f; co = 1.0f; return; }
+    const float d = Real<float>::sqrt_(d2);
+    float s;
+    Real<float>::sincos_(0.5f * d, &s, &co);
+    f = s / d;
+}
+TCYM_HD void half_angle(double d2, double &f, double &co) {
+    if (d2 == 0.0) { f = 0.5; co = 1.0; return; }
+    const double d = Real<double>::sqrt_(d2);
+    double s;
+    Real<double>::sincos_(0.5 * d, &s, &co);
+    f = s / d;
+}
+TCYM_HD void half_angle(f2 d2, f2 &f, f2 &co) {  // no packed sine: lane by lane
+    half_angle(d2.v.x, f.v.x, co.v.x);
+    half_angle(d2.v.y, f.v.y, co.v.y);
+}
+
 template <class T> struct cx {
     T re, im;
 };
@@ -119,9 +189,8 @@ template <class T> struct SU2 {
     // quaternion product (u3 + i u.s)(v3 + i v.s) = u3 v3 - u.v + i (u3 v + v3 u - u x v).s
     // with optional conjugation of either factor
     template <bool DA, bool DB> static TCYM_HD Mat mulx(const Mat &a, const Mat &b) {
-        const T sa = DA ? T(-1) : T(1), sb = DB ? T(-1) : T(1);
-        T u0 = sa * a.q[0], u1 = sa * a.q[1], u2 = sa * a.q[2], u3 = a.q[3];
-        T v0 = sb * b.q[0], v1 = sb * b.q[1], v2 = sb * b.q[2], v3 = b.q[3];
+        const T u0 = DA ? -a.q[0] : a.q[0], u1 = DA ? -a.q[1] : a.q[1], u2 = DA ? -a.q[2] : a.q[2], u3 = a.q[3];
+        const T v0 = DB ? -b.q[0] : b.q[0], v1 = DB ? -b.q[1] : b.q[1], v2 = DB ? -b.q[2] : b.q[2], v3 = b.q[3];
         Mat w;
         w.q[0] = fma(u3, v0, fma(v3, u0, -(u1 * v2 - u2 * v1)));
         w.q[1] = fma(u3, v1, fma(v3, u1, -(u2 * v0 - u0 * v2)));
@@ -144,11 +213,8 @@ template <class T> struct SU2 {
     static TCYM_HD Mat iexp(T c, const T *e) {
         T x0 = c * e[0], x1 = c * e[1], x2 = c * e[2];
         T d2 = fma(x0, x0, fma(x1, x1, x2 * x2));
-        if (d2 == T(0)) return identity();
-        T d = Real<T>::sqrt_(d2);
-        T s, co;
-        Real<T>::sincos_(T(0.5) * d, &s, &co);
-        T f = s / d;
+        T f, co;
+        half_angle(d2, f, co);
         return Mat{{f * x0, f * x1, f * x2, co}};
     }
     // components of V (e^k t^k) V^dagger: the pure quaternion (e,0) rotated
@@ -404,7 +470,10 @@ template <class T> struct SU3 {
         const T o02 = q.m[0][2].re * q.m[0][2].re + q.m[0][2].im * q.m[0][2].im;
         const T o12 = q.m[1][2].re * q.m[1][2].re + q.m[1][2].im * q.m[1][2].im;
         const T c1 = T(0.5) * (d0 * d0 + d1 * d1 + d2 * d2) + (o01 + o02 + o12);
-        if (c1 * T(4.0 / 3.0) > T(0.25)) return mulu<false, false>(iexp_hermitian(q), u);
+        if (any_gt(c1 * T(4.0 / 3.0), T(0.25))) {
+            if constexpr (Packed<T>::value) return iexp_mul_lanes(c, e, u);
+            else return mulu<false, false>(iexp_hermitian(q), u);
+        }
         // rows 0 and 1 of Q^2 (Hermitian Q)
         cx<T> q2[2][3];
 #pragma unroll
@@ -435,6 +504,30 @@ template <class T> struct SU3 {
                 w.m[i][j] = cx<T>{re, im};
             }
         return mulu<false, false>(w, u);  // reads rows 0 and 1 of w only
+    }
+    // packed pairs whose exponent needs scaling: each lane through the scalar path
+    template <class P = T> static TCYM_HD Mat iexp_mul_lanes(P c, const P *e, const Mat &u) {
+        Mat r;
+#pragma unroll
+        for (int l = 0; l < 2; ++l) {
+            float el[NA];
+            typename SU3<float>::Mat ul;
+#pragma unroll
+            for (int a = 0; a < NA; ++a) el[a] = lane(e[a], l);
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int j = 0; j < 3; ++j) ul.m[i][j] = cx<float>{lane(u.m[i][j].re, l), lane(u.m[i][j].im, l)};
+            const typename SU3<float>::Mat w = SU3<float>::iexp_mul(lane(c, l), el, ul);
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int j = 0; j < 3; ++j) {
+                    if (l == 0) { r.m[i][j].re.v.x = w.m[i][j].re; r.m[i][j].im.v.x = w.m[i][j].im; }
+                    else { r.m[i][j].re.v.y = w.m[i][j].re; r.m[i][j].im.v.y = w.m[i][j].im; }
+                }
+        }
+        return r;
     }
 
     // f_k of exp(iQ) = f0 + f1 Q + f2 Q^2 for spectral radius <= 1/2: the Taylor
@@ -487,9 +580,14 @@ template <class T> struct SU3 {
     // third row of an SU(3) matrix from the first two: r2 = conj(r0 x r1)
     static TCYM_HD void complete_row2(Mat &u) {
         const cx<T> *a = u.m[0], *b = u.m[1];
-        u.m[2][0] = conj(a[1] * b[2] - a[2] * b[1]);
-        u.m[2][1] = conj(a[2] * b[0] - a[0] * b[2]);
-        u.m[2][2] = conj(a[0] * b[1] - a[1] * b[0]);
+        u.m[2][0] = conj_cross(a[1], b[2], a[2], b[1]);
+        u.m[2][1] = conj_cross(a[2], b[0], a[0], b[2]);
+        u.m[2][2] = conj_cross(a[0], b[1], a[1], b[0]);
+    }
+    // conj(x y - z w) as fused multiply-adds
+    static TCYM_HD cx<T> conj_cross(cx<T> x, cx<T> y, cx<T> z, cx<T> w) {
+        return {fma(x.re, y.re, fma(-x.im, y.im, fma(-z.re, w.re, z.im * w.im))),
+                fma(z.re, w.im, fma(z.im, w.re, fma(-x.re, y.im, -(x.im * y.re))))};
     }
     // Gram-Schmidt of rows 0 and 1, row 2 rebuilt: the nearest SU(3) matrix
     // for a link that has drifted by rounding (not a max-trace projection).

@@ -42,7 +42,8 @@ size_t footprint_of(const tcym_request &r, int sm_count) {
     const int fmt = tcym_format_of(r.nc, r.precision);
     const size_t V = (size_t)r.L * r.L * r.L;
     const size_t na = r.nc == 2 ? 3 : 8;
-    return 2 * 3 * tcym_link_bytes(fmt) * V + 3 * tcym_field_bytes(fmt) * V + sizeof(double) * na * V  // restore scratch
+    const size_t nst = tcym_stored_sites(fmt, (int64_t)V);
+    return 2 * 3 * tcym_link_bytes(fmt) * nst + 3 * tcym_field_bytes(fmt) * nst + sizeof(double) * na * V  // restore scratch
            + sizeof(double) * (12 * (size_t)sm_count * 8 + 16) + 8 * 32 * ((V + 255) / 256);                  // reductions
 }
 

@@ -102,6 +102,79 @@ TCYM_HD void site_step(const Geom &g, const void *Uin, void *Uout, void *E, cons
     }
 }
 
+// ------------------------------------------------------------------ site pairs
+// site_step for both sites of pair p of an FP32 lattice with even nz, (x,y,z)
+// and (x,y,z+nz/2), in packed FP32 (f2): the same staples, projection, E
+// update and exponential per lane, at half the instructions.  SEAM: the pair
+// may touch the seam z = nz/2, across which neighbour pairs arrive with their
+// lanes swapped; pairs away from it skip the swap tests.
+template <class F, bool SEAM>
+TCYM_HD typename F::Mat2 staple_sum_pair(const void *U, int64_t Vh, const PairNbhd &nb, int mu,
+                                         const float (&cnu)[3]) {
+    using G2 = typename F::G2;
+    using M2 = typename F::Mat2;
+    M2 A = G2::zero();
+#pragma unroll
+    for (int k = 1; k <= 2; ++k) {
+        const int nu = mu + k >= 3 ? mu + k - 3 : mu + k;
+        M2 a1 = F::load2(U, Vh, nu, nb.at(mu, 1), SEAM && nb.swapped(mu, 1));
+        M2 a2 = F::load2(U, Vh, mu, nb.at(nu, 1), SEAM && nb.swapped(nu, 1));
+        M2 a3 = F::load2(U, Vh, nu, nb.p, false);
+        M2 up = G2::template mulu<false, true>(G2::template mulu<false, true>(a1, a2), a3);
+        M2 b1 = F::load2(U, Vh, nu, nb.at(mu, 1, nu, -1), SEAM && nb.swapped(mu, 1, nu, -1));
+        const int64_t sb = nb.at(nu, -1);
+        const bool wb = SEAM && nb.swapped(nu, -1);
+        M2 b2 = F::load2(U, Vh, mu, sb, wb);
+        M2 b3 = F::load2(U, Vh, nu, sb, wb);
+        M2 lo = G2::template mulu<false, false>(G2::template mulu<true, true>(b1, b2), b3);
+        A = G2::add(A, G2::scale(f2(sel3(cnu, nu)), G2::add(up, lo)));
+    }
+    return A;
+}
+
+template <class F, bool SEAM>
+TCYM_HD void site_step_pair(const Geom &g, const void *Uin, void *Uout, void *E, const StepCoef<float> &c, int64_t p,
+                            uint64_t step_add = 0) {
+    using G2 = typename F::G2;
+    using M2 = typename F::Mat2;
+    constexpr int NA = F::NA;
+    const int64_t Vh = g.V >> 1;
+    const PairNbhd nb(g, p);
+#pragma unroll 1
+    for (int mu = 0; mu < 3; ++mu) {
+        f2 e[NA];
+        F::load_e2(E, Vh, mu, p, e);
+        const M2 u = F::load2(Uin, Vh, mu, p, false);
+        const M2 A = staple_sum_pair<F, SEAM>(Uin, Vh, nb, mu, c.cnu);
+        f2 f[NA];
+        G2::proj_mul(u, A, f);
+        const f2 fc(sel3(c.fc, mu));
+        if (c.mode == MODE_LANGEVIN) {
+            float x0[NA], x1[NA];
+            normals<float, NA>(c.seed, STREAM_NOISE, c.step + step_add, (uint32_t)p, (uint32_t)mu, x0);
+            normals<float, NA>(c.seed, STREAM_NOISE, c.step + step_add, (uint32_t)(p + Vh), (uint32_t)mu, x1);
+            const f2 damp(sel3(c.damp, mu)), kick(sel3(c.kick, mu));
+#pragma unroll
+            for (int a = 0; a < NA; ++a) e[a] = e[a] + fma(kick, f2(x0[a], x1[a]), fma(-damp, e[a], fc * f[a]));
+        } else if (c.mode == MODE_FLOW) {
+#pragma unroll
+            for (int a = 0; a < NA; ++a) e[a] = fc * f[a];
+        } else {
+#pragma unroll
+            for (int a = 0; a < NA; ++a) e[a] = fma(fc, f[a], e[a]);
+        }
+        F::store_e2(E, Vh, mu, p, e);
+        F::store2(Uout, Vh, mu, p, G2::iexp_mul(f2(sel3(c.uc, mu)), e, u));
+    }
+}
+
+// Does the block of pairs [p0, p0 + n) touch the seam planes z = 0 or z = nz/2 - 1?
+TCYM_HD bool pairs_touch_seam(const Geom &g, int64_t p0, int64_t n) {
+    const int64_t Vh = g.V >> 1, plane = (int64_t)g.nx * g.ny;
+    const int64_t last = (p0 + n < Vh ? p0 + n : Vh) - 1;
+    return p0 < plane || last >= Vh - plane;
+}
+
 // Checkerboard flow: one link U_mu(x) of the active parity moved in place by
 // exp(-i dtau F_mu(x)), F = fc proj(U_mu A) (no reference counterpart; the
 // reference flows all links at once, GradientFlow.cpp:150-165).
