@@ -127,6 +127,15 @@ int tcym_set_zero(tcym_lattice lat);
  * sigma = 1/sqrt(beta) this is ThermalDynamics::ReassignElectricFields before its
  * Gauss restore (DYNAMICS/ThermalDynamics.cpp:205-226). */
 int tcym_gaussian_efield(tcym_lattice lat, double sigma, uint64_t seed);
+/* ThermalDynamics::Thermalize(rounds, max_time) (DYNAMICS/ThermalDynamics.cpp:260-314):
+ * `rounds` times, E = N(0,1)/sqrt(beta) (round r: field stream step r), Gauss
+ * restore (restore_tol <= 0: 1e-14 in FP64, 1e-6 in FP32; at most 10000 sweeps),
+ * then leapfrog steps of dt while steps*dt < max_time (the reference: dt 0.0375).
+ * Every `every` steps (the reference: 20) one record of 7 doubles is written to
+ * series (up to series_cap records; *records gets the count): t + r*max_time,
+ * T00, TXX, TYY, TZZ, ELECTRIC, MAGNETIC, the reference's ThermalEnergy line. */
+int tcym_thermalize(tcym_lattice lat, double beta, uint64_t seed, int rounds, double max_time, double dt,
+                    double restore_tol, int every, double *series, int series_cap, int *records);
 /* U_mu(x) = exp(i t^a theta^a), theta^a = sigma * N(0,1) from the Philox link stream. */
 int tcym_random_links(tcym_lattice lat, double sigma, uint64_t seed);
 /* GaussLawRestoration::Restore (GAUSSLAWFIXING/GaussRestore.cpp:131-167): iterate

@@ -22,6 +22,7 @@
 
 #include <cmath>
 #include <complex>
+#include <fstream>
 #include <cstring>
 #include <iostream>
 #include <stdexcept>
@@ -329,8 +330,13 @@ namespace RandomNumberGenerator {
 inline long int MySEED = 0;  // seeds the Philox streams of the compat layer
 }
 
+namespace IO {
+inline std::string OutputDirectory;  // with a trailing '/', as IO/OutputManagement.cpp sets it
+}
+
 namespace ThermalDynamics {
 inline DOUBLE beta = 2.0;
+inline DOUBLE dTau = 0.0375;  // static const in DYNAMICS/ThermalDynamics.cpp:23
 }
 
 namespace GaussLawRestoration {
@@ -354,6 +360,25 @@ inline void ReassignElectricFields() {
     tcym_compat::check(tcym_gaussian_efield(lat, 1.0 / std::sqrt(beta), (uint64_t)RandomNumberGenerator::MySEED),
                        "Gaussian fields");
     GaussLawRestoration::Restore(GLinks::U, EFields::E);
+}
+// Thermalize(MaxSteps, MaxTime) (DYNAMICS/ThermalDynamics.cpp:260-314), writing the
+// energy series to <OutputDirectory>ThermalEnergyID<seed>.txt as the reference does
+inline void Thermalize(INT MaxSteps, DOUBLE MaxTime) {
+    long steps = 0;
+    while ((double)steps * dTau < MaxTime) ++steps;
+    std::vector<double> series(7 * (size_t)MaxSteps * (size_t)(steps / 20 + 1));
+    int n = 0;
+    tcym_compat::check(tcym_thermalize(tcym_compat::bind(GLinks::U, EFields::E), beta,
+                                       (uint64_t)RandomNumberGenerator::MySEED, (int)MaxSteps, MaxTime, dTau, 0.0,
+                                       20, series.data(), (int)(series.size() / 7), &n),
+                       "thermalize");
+    std::ofstream out(IO::OutputDirectory + "ThermalEnergyID" + std::to_string(RandomNumberGenerator::MySEED) +
+                      ".txt");
+    out.precision(15);
+    for (int i = 0; i < n; ++i) {
+        for (int k = 0; k < 7; ++k) out << (k ? " " : "") << series[7 * (size_t)i + k];
+        out << "\n";
+    }
 }
 }  // namespace ThermalDynamics
 

@@ -83,6 +83,10 @@ class Port:
         f("edotb_improved").restype = ctypes.c_double
         f("set_zero").argtypes = [_int_p, _dbl_p, _dbl_p]
         f("gaussian_efield").argtypes = [_int_p, _dbl_p, ctypes.c_double, ctypes.c_uint64]
+        f("gaussian_efield_step").argtypes = [_int_p, _dbl_p, ctypes.c_double, ctypes.c_uint64, ctypes.c_uint64]
+        f("thermalize").argtypes = [_int_p, _dbl_p, _dbl_p, ctypes.c_double, ctypes.c_uint64, ctypes.c_int,
+                                    ctypes.c_double, ctypes.c_double, ctypes.c_int, _dbl_p, ctypes.c_int]
+        f("thermalize").restype = ctypes.c_int
         f("random_links").argtypes = [_int_p, _dbl_p, ctypes.c_double, ctypes.c_uint64]
         f("matrix_iexp").argtypes = [ctypes.c_double, _dbl_p, _dbl_p]
         f("retr_igen").argtypes = [_dbl_p, _dbl_p]
@@ -134,6 +138,15 @@ class Port:
 
     def gaussian_efield(self, shape, E, sigma, seed):
         self._f("gaussian_efield")(_n(shape), _p(E), sigma, seed)
+
+    def gaussian_efield_step(self, shape, E, sigma, seed, step):
+        self._f("gaussian_efield_step")(_n(shape), _p(E), sigma, seed, step)
+
+    def thermalize(self, shape, U, E, beta, seed, rounds, max_time, dt=0.0375, every=20, cap=100000):
+        """ThermalDynamics::Thermalize; returns the (records, 7) energy series."""
+        series = np.zeros((cap, 7))
+        n = self._f("thermalize")(_n(shape), _p(U), _p(E), beta, seed, rounds, max_time, dt, every, _p(series), cap)
+        return series[:n].copy()
 
     def random_links(self, shape, U, sigma, seed):
         self._f("random_links")(_n(shape), _p(U), sigma, seed)
@@ -194,6 +207,8 @@ class Ref:
         L.ref_flow.argtypes = [ctypes.c_double, ctypes.c_int, ctypes.c_int]
         L.ref_flow.restype = ctypes.c_double
         L.ref_thermal_efield.argtypes = [ctypes.c_double, ctypes.c_uint64]
+        L.ref_thermalize.argtypes = [ctypes.c_double, ctypes.c_uint64, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                     ctypes.c_char_p]
         L.ref_observables.argtypes = [_dbl_p]
         L.ref_matrix_iexp.argtypes = [ctypes.c_double, _dbl_p, _dbl_p]
         L.ref_retr_igen.argtypes = [_dbl_p, _dbl_p]
@@ -241,6 +256,13 @@ class Ref:
         out = np.zeros(16)
         self.lib.ref_observables(_p(out))
         return out
+
+    def thermalize(self, beta, seed, rounds, max_time, dtau, outdir):
+        """ThermalDynamics::Thermalize; returns the (records, 7) series it writes to
+        <outdir>/ThermalEnergyID<seed>.txt."""
+        import os
+        self.lib.ref_thermalize(beta, seed, rounds, max_time, dtau, str(outdir).encode())
+        return np.loadtxt(os.path.join(str(outdir), f"ThermalEnergyID{seed}.txt"), ndmin=2)
 
     def matrix_iexp(self, c, alpha):
         out = np.zeros(NM[self.nc])

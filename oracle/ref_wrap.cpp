@@ -41,19 +41,24 @@ namespace RandomNumberGenerator {
     static uint32_t shim_stream = 0;
     static uint64_t shim_step = 0;
     static uint64_t shim_index = 0;
+    static uint64_t shim_field = 0;  /* E components of the lattice: 3 * NA * V (set by ref_init) */
 
     void Init(long int SEED) { MySEED = SEED; shim_seed = (uint64_t)SEED; shim_index = 0; }
     void SetStream(uint64_t seed, uint32_t stream, uint64_t step) {
         shim_seed = seed; shim_stream = stream; shim_step = step; shim_index = 0;
     }
-    /* The i-th call returns the normal of E component i = a + NA*(mu + 3*site). */
+    /* The i-th call returns the normal of E component i = a + NA*(mu + 3*site); each
+     * further whole field's worth of calls (a later ReassignElectricFields, as in
+     * ThermalDynamics::Thermalize) moves on to the next step of the stream. */
     DOUBLE Gauss() {
         const uint64_t na = SUNcAlgebra::VectorSize;
         uint64_t i = shim_index++;
+        uint64_t round = 0;
+        if (shim_field) { round = i / shim_field; i %= shim_field; }
         uint32_t a = (uint32_t)(i % na);
         uint32_t mu = (uint32_t)((i / na) % 3);
         uint32_t site = (uint32_t)(i / (3 * na));
-        return orc_normal(shim_seed, shim_stream, shim_step, site, mu, a);
+        return orc_normal(shim_seed, shim_stream, shim_step + round, site, mu, a);
     }
     DOUBLE Gauss(DOUBLE Amplitude) { return Amplitude * Gauss(); }
     DOUBLE rng() { std::fprintf(stderr, "oracle: uniform RNG is off the hot path\n"); std::abort(); }
@@ -107,6 +112,7 @@ void ref_init(int nx, int ny, int nz) {
     if (GLinks::U) { delete GLinks::U; delete EFields::E; }
     Lattice::N[0] = nx; Lattice::N[1] = ny; Lattice::N[2] = nz;
     Lattice::Volume = nx * ny * nz;
+    RandomNumberGenerator::shim_field = 3ull * SUNcAlgebra::VectorSize * (uint64_t)Lattice::Volume;
     Lattice::Init();
     Dynamics::Reset();
     LangevinDynamics::Reset();
@@ -181,6 +187,19 @@ void ref_thermal_efield(double beta, uint64_t seed) {
     ThermalDynamics::beta = beta;
     RandomNumberGenerator::SetStream(seed, ORC_STREAM_EFIELD, 0);
     ThermalDynamics::ReassignElectricFields();
+}
+
+/* ThermalDynamics::Thermalize(rounds, max_time) (DYNAMICS/ThermalDynamics.cpp:260-314)
+ * with ThermalDynamics::dTau = dtau, writing its energy series to
+ * <outdir>/ThermalEnergyID<seed>.txt as the reference does. */
+void ref_thermalize(double beta, uint64_t seed, int rounds, double max_time, double dtau, const char *outdir) {
+    IO::OutputDirectory = StringManipulation::StringCast(outdir, "/");
+    ThermalDynamics::beta = beta;
+    ThermalDynamics::dTau = dtau;
+    ThermalDynamics::Reset();
+    RandomNumberGenerator::MySEED = (long int)seed;
+    RandomNumberGenerator::SetStream(seed, ORC_STREAM_EFIELD, 0);
+    ThermalDynamics::Thermalize(rounds, max_time);
 }
 
 /* Observables: Bulk (OBSERVABLES/BulkObservables.cpp:133-143), GaussLaw

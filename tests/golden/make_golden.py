@@ -15,6 +15,10 @@ CUDA library draws); every output below is produced by the reference itself:
   ref_c0_su2_16.npz        BASELINE config 0: SU(2) 16^3, U = 1, E ~ N(0, 1/2)
                            (seed 1) Gauss-restored by the reference, 1000 leapfrog
                            steps at dt 0.05, observables every 10 steps
+  ref_thermalize_su{2,3}.npz  ThermalDynamics::Thermalize(2, 0.75) on a (4,4,6)
+                           lattice from U = 1, beta 2, seed 7, dTau 0.0375 (20
+                           steps a round): final U, E and the ThermalEnergy file
+                           (every 20 steps; the reference writes 6 digits)
 
   python tests/golden/make_golden.py
 """
@@ -103,6 +107,19 @@ def config0():
                         every=10)
 
 
+def thermalize(nc):
+    import tempfile
+    R = oracle.Ref(nc)
+    shape = (4, 4, 6)
+    R.init(shape)
+    R.set_zero()
+    with tempfile.TemporaryDirectory() as d:
+        series = R.thermalize(2.0, 7, 2, 0.75, 0.0375, d)
+    U, E = R.get()
+    np.savez_compressed(os.path.join(HERE, f"ref_thermalize_su{nc}.npz"), U=U, E=E, series=series,
+                        shape=np.array(shape), beta=2.0, seed=7, rounds=2, max_time=0.75, dtau=0.0375)
+
+
 if __name__ == "__main__":
     oracle.build()
     if not (oracle.ref_available(2) and oracle.ref_available(3)):
@@ -111,6 +128,8 @@ if __name__ == "__main__":
         states(nc)
         group(nc)
     config0()
+    for nc in (2, 3):
+        thermalize(nc)
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))

@@ -37,12 +37,19 @@ def test_leapfrog_parity(ctx, oracle_port, nc, prec, shape):
     lat = tcym.Lattice(ctx, nc, shape, prec)
     lat.set_reunitarize_period(0)
     lat.upload(U, E)
-    for nsteps in (1, 9, 90):  # cumulative 1, 10, 100 steps at dt = 0.05
+    for total, nsteps in ((1, 1), (10, 9), (100, 90)):  # cumulative steps at dt = 0.05
         lat.leapfrog(0.05, nsteps)
         P.leapfrog(shape, U, E, 0.05, nsteps)
         Ug, Eg = lat.download()
-        assert rel(Ug, U) < TOL[prec], (nsteps, rel(Ug, U))
-        assert rel(Eg, E) < TOL[prec], (nsteps, rel(Eg, E))
+        tol = TOL[prec]
+        if prec == tcym.FP32 and total == 100:
+            # this rough random start (sigma_U = 0.6) is chaotic enough to amplify the
+            # FP32 storage rounding ~6x per 50 steps (1.3e-6 at step 50, 8e-6..1e-5 at
+            # 100, the same for the host build of the paired and the per-site step);
+            # the configurations' own starts keep 1e-5 over 100 steps (test_gpu_configs)
+            tol = 3e-5
+        assert rel(Ug, U) < tol, (total, rel(Ug, U))
+        assert rel(Eg, E) < tol, (total, rel(Eg, E))
 
 
 @pytest.mark.parametrize("prec", PREC)
@@ -210,3 +217,23 @@ def test_error_codes(ctx):
     with pytest.raises(tcym.TcymError) as ei:
         lat.flow(0.01, 1, tcym.FLOW_CHECKERBOARD)  # odd extent
     assert ei.value.code == 1
+
+
+@pytest.mark.parametrize("prec", PREC)
+@pytest.mark.parametrize("nc", GROUPS)
+def test_thermalize_parity(ctx, oracle_port, nc, prec):
+    """tcym_thermalize against the oracle's ThermalDynamics::Thermalize (2 rounds of
+    20 steps at dTau 0.0375 from U = 1, records every 5 steps)."""
+    shape = (6, 4, 6)
+    P = oracle_port[nc]
+    U, E = oracle.empty_fields(nc, shape)
+    P.set_zero(shape, U, E)
+    ref = P.thermalize(shape, U, E, 2.0, 7, 2, 0.75, 0.0375, 5)
+    lat = tcym.Lattice(ctx, nc, shape, prec)
+    lat.set_zero()
+    series = lat.thermalize(2.0, 7, 2, 0.75, 0.0375, every=5)
+    assert series.shape == ref.shape == (8, 7)
+    tol = TOL[prec] if prec == tcym.FP64 else 2e-5  # FP32 restores to 1e-6 before the steps
+    assert np.abs(series - ref).max() <= tol * np.abs(ref).max()
+    Ug, Eg = lat.download()
+    assert rel(Ug, U) < tol and rel(Eg, E) < tol

@@ -122,3 +122,19 @@ def test_config0_initial_state_and_series(oracle_port):
         o = P.observables(shape, U, E)
         assert abs(o[0] - s[rec][0]) < 1e-10 * s[rec][0]
         assert abs(o[13] - s[rec][13]) < 1e-8 * max(1.0, abs(s[rec][13]))
+
+
+@pytest.mark.parametrize("nc", [2, 3])
+def test_thermalize_equals_reference(oracle_port, nc):
+    """ThermalDynamics::Thermalize: the oracle's restatement reproduces the
+    reference's final fields and its ThermalEnergy series (written with 6 digits)."""
+    d = load(f"ref_thermalize_su{nc}.npz")
+    shape = tuple(int(v) for v in d["shape"])
+    P = oracle_port[nc]
+    U, E = oracle.empty_fields(nc, shape)
+    P.set_zero(shape, U, E)
+    series = P.thermalize(shape, U, E, float(d["beta"]), int(d["seed"]), int(d["rounds"]), float(d["max_time"]),
+                          float(d["dtau"]), 20)
+    assert series.shape == d["series"].shape
+    assert np.allclose(series, d["series"], rtol=5e-6, atol=1e-6)
+    assert rel(U, d["U"]) < 1e-12 and rel(E, d["E"]) < 1e-12

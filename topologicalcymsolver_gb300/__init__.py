@@ -119,6 +119,9 @@ def library() -> ctypes.CDLL:
         "tcym_lattice_stream": ([ctypes.c_void_p, c_void_pp], ctypes.c_int),
         "tcym_set_zero": ([ctypes.c_void_p], ctypes.c_int),
         "tcym_gaussian_efield": ([ctypes.c_void_p, ctypes.c_double, ctypes.c_uint64], ctypes.c_int),
+        "tcym_thermalize": ([ctypes.c_void_p, ctypes.c_double, ctypes.c_uint64, ctypes.c_int, ctypes.c_double,
+                             ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
+                             ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
         "tcym_random_links": ([ctypes.c_void_p, ctypes.c_double, ctypes.c_uint64], ctypes.c_int),
         "tcym_gauss_restore": ([ctypes.c_void_p, ctypes.c_double, ctypes.c_int, ctypes.POINTER(ctypes.c_int), _dp],
                                ctypes.c_int),
@@ -261,6 +264,19 @@ class Lattice:
 
     def gaussian_efield(self, sigma: float, seed: int):
         self.ctx.check(self.lib.tcym_gaussian_efield(self.h, sigma, seed))
+
+    def thermalize(self, beta: float, seed: int, rounds: int, max_time: float, dt: float = 0.0375,
+                   every: int = 20, restore_tol: float = 0.0) -> np.ndarray:
+        """ThermalDynamics::Thermalize; returns the (records, 7) ThermalEnergy series."""
+        steps = 0
+        while steps * dt < max_time:
+            steps += 1
+        cap = max(1, rounds * (steps // every if every > 0 else 0))
+        series = np.zeros((cap, 7))
+        n = ctypes.c_int(0)
+        self.ctx.check(self.lib.tcym_thermalize(self.h, beta, seed, rounds, max_time, dt, restore_tol, every,
+                                                series.ctypes.data_as(ctypes.c_void_p), cap, ctypes.byref(n)))
+        return series[:n.value].copy()
 
     def random_links(self, sigma: float, seed: int):
         self.ctx.check(self.lib.tcym_random_links(self.h, sigma, seed))

@@ -327,7 +327,7 @@ extern "C" int tcym_gaussian_efield(tcym_lattice lat, double sigma, uint64_t see
     if (!lat) return TCYM_ERR_ARG;
     tcym_ctx ctx = lat->ctx;
     cudaSetDevice(ctx->device);
-    DISPATCH(lat->fmt, CK(L::gaussian_efield(lat->g, lat->E, sigma, seed, lat->stream)));
+    DISPATCH(lat->fmt, CK(L::gaussian_efield(lat->g, lat->E, sigma, seed, 0, lat->stream)));
     return TCYM_OK;
 }
 
@@ -395,6 +395,55 @@ extern "C" int tcym_gauss_restore(tcym_lattice lat, double tol, int maxit, int *
     }
     if (iters) *iters = it;
     if (final_max) *final_max = gmax;
+    return TCYM_OK;
+}
+
+// ThermalDynamics::Thermalize(rounds, max_time) (DYNAMICS/ThermalDynamics.cpp:260-314):
+// each round redraws E = N(0,1)/sqrt(beta) (round r draws the field stream at
+// step r, ReassignElectricFields :205-226), restores Gauss's law, and runs the
+// leapfrog (ThermalDynamics::Update, :238-249) while t = steps * dt < max_time,
+// the clock restarting each round (:274, :294).  Every `every` steps it appends
+// the reference's ThermalEnergy record (:280-285): t + r max_time, T00, TXX,
+// TYY, TZZ, ELECTRIC, MAGNETIC (BulkObservables.cpp:29-52).
+extern "C" int tcym_thermalize(tcym_lattice lat, double beta, uint64_t seed, int rounds, double max_time, double dt,
+                               double restore_tol, int every, double *series, int series_cap, int *records) {
+    if (!lat || !(beta > 0) || rounds < 0 || !(dt > 0) || every < 0 || series_cap < 0 ||
+        (series_cap > 0 && !series))
+        return TCYM_ERR_ARG;
+    tcym_ctx ctx = lat->ctx;
+    cudaSetDevice(ctx->device);
+    // the reference restores to 1e-14 (GaussRestore.cpp:150); FP32 storage holds ~1e-6
+    const double tol = restore_tol > 0 ? restore_tol : (lat->precision == TCYM_FP64 ? 1e-14 : 1e-6);
+    int nrec = 0, rc = 0;
+    if (records) *records = 0;
+    for (int r = 0; r < rounds; ++r) {
+        DISPATCH(lat->fmt, CK(L::gaussian_efield(lat->g, lat->E, 1.0 / std::sqrt(beta), seed, (uint64_t)r,
+                                                 lat->stream)));
+        if ((rc = tcym_gauss_restore(lat, tol, 10000, nullptr, nullptr))) return rc;
+        long nsteps = 0;  // steps of the round: the reference's while (Time() < MaxTime)
+        while ((double)nsteps * dt < max_time) ++nsteps;
+        long done = 0;
+        while (done < nsteps) {
+            const long next = every > 0 ? std::min(nsteps, (done / every + 1) * every) : nsteps;
+            if ((rc = tcym_run_steps(lat, MODE_LEAPFROG, dt, 0, 0, 0, 0, (int)(next - done)))) return rc;
+            done = next;
+            if (every > 0 && done % every == 0 && nrec < series_cap) {
+                if ((rc = tcym_reduce(lat, OBS_BULK, 0.0)) || (rc = fetch_result(lat))) return rc;
+                const double *h = lat->host_result;
+                const double e0 = h[R_ESQ0], e1 = h[R_ESQ0 + 1], e2 = h[R_ESQ0 + 2];
+                const double b0 = h[R_BSQ0], b1 = h[R_BSQ0 + 1], b2 = h[R_BSQ0 + 2];
+                double *rec = series + 7 * (size_t)nrec++;
+                rec[0] = (double)done * dt + r * max_time;
+                rec[1] = 0.5 * (e0 + e1 + e2 + b0 + b1 + b2);
+                rec[2] = 0.5 * ((e1 + e2 + b1 + b2) - (e0 + b0));
+                rec[3] = 0.5 * ((e0 + e2 + b0 + b2) - (e1 + b1));
+                rec[4] = 0.5 * ((e0 + e1 + b0 + b1) - (e2 + b2));
+                rec[5] = 0.5 * (e0 + e1 + e2);
+                rec[6] = 0.5 * (b0 + b1 + b2);
+                if (records) *records = nrec;
+            }
+        }
+    }
     return TCYM_OK;
 }
 

@@ -45,11 +45,16 @@ template <int FMT> constexpr int threads_for() { return Fmt<FMT>::NA == 3 ? kThr
 // The paired step (FP32 formats, even nz): one thread per site pair, 128 per
 // block; resident blocks per SM requested (register cap 65536 / (blocks * 128)).
 constexpr int kThreadsPair = 128;
+// 1: blocks away from the seam run a copy of the step without the lane-swap
+// tests; 0: one copy, the swaps decided per load
+#ifndef TCYM_PAIR_SEAM_SPLIT
+#define TCYM_PAIR_SEAM_SPLIT 1
+#endif
 #ifndef TCYM_SU3_PAIR_MINBLOCKS
 #define TCYM_SU3_PAIR_MINBLOCKS 2
 #endif
 #ifndef TCYM_SU2_PAIR_MINBLOCKS
-#define TCYM_SU2_PAIR_MINBLOCKS 4
+#define TCYM_SU2_PAIR_MINBLOCKS 6
 #endif
 template <int FMT> constexpr int pair_min_blocks_for() {
     return Fmt<FMT>::NA == 8 ? TCYM_SU3_PAIR_MINBLOCKS : TCYM_SU2_PAIR_MINBLOCKS;
@@ -88,8 +93,12 @@ __global__ void __launch_bounds__(kThreadsPair, pair_min_blocks_for<FMT>())
     k_step_pair(Geom g, const void *Uin, void *Uout, void *E, StepCoef<float> c) {
     const int64_t p0 = (int64_t)blockIdx.x * blockDim.x, p = p0 + threadIdx.x;
     if (p >= (g.V >> 1)) return;
+#if TCYM_PAIR_SEAM_SPLIT
     if (pairs_touch_seam(g, p0, blockDim.x)) site_step_pair<Fmt<FMT>, true>(g, Uin, Uout, E, c, p);
     else site_step_pair<Fmt<FMT>, false>(g, Uin, Uout, E, c, p);
+#else
+    site_step_pair<Fmt<FMT>, true>(g, Uin, Uout, E, c, p);
+#endif
 }
 
 // sites of parity p, for even extents: t -> (x, row) with x of the right parity
@@ -199,9 +208,9 @@ template <int FMT> __global__ void k_set_zero(Geom g, void *U, void *E) {
     int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (s < g.V) site_set_zero<Fmt<FMT>>(g, U, E, s);
 }
-template <int FMT> __global__ void k_gaussian_efield(Geom g, void *E, double sigma, uint64_t seed) {
+template <int FMT> __global__ void k_gaussian_efield(Geom g, void *E, double sigma, uint64_t seed, uint64_t step) {
     int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (s < g.V) site_gaussian_efield<Fmt<FMT>>(g, E, sigma, seed, s);
+    if (s < g.V) site_gaussian_efield<Fmt<FMT>>(g, E, sigma, seed, s, step);
 }
 template <int FMT> __global__ void k_random_links(Geom g, void *U, double sigma, uint64_t seed) {
     int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -271,8 +280,9 @@ template <int FMT> struct Launch {
         k_set_zero<FMT><<<grid_for(g.V, 256), 256, 0, st>>>(g, U, E);
         return cudaGetLastError();
     }
-    static cudaError_t gaussian_efield(const Geom &g, void *E, double sigma, uint64_t seed, cudaStream_t st) {
-        k_gaussian_efield<FMT><<<grid_for(g.V, 128), 128, 0, st>>>(g, E, sigma, seed);
+    static cudaError_t gaussian_efield(const Geom &g, void *E, double sigma, uint64_t seed, uint64_t step,
+                                       cudaStream_t st) {
+        k_gaussian_efield<FMT><<<grid_for(g.V, 128), 128, 0, st>>>(g, E, sigma, seed, step);
         return cudaGetLastError();
     }
     static cudaError_t random_links(const Geom &g, void *U, double sigma, uint64_t seed, cudaStream_t st) {

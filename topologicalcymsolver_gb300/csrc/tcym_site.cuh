@@ -103,6 +103,10 @@ TCYM_HD void site_step(const Geom &g, const void *Uin, void *Uout, void *E, cons
 }
 
 // ------------------------------------------------------------------ site pairs
+#ifndef TCYM_PAIR_STAPLE_UNROLL
+#define TCYM_PAIR_STAPLE_UNROLL 2
+#endif
+constexpr int kPairStapleUnroll = TCYM_PAIR_STAPLE_UNROLL;  // 1: one copy of the staple code for both planes
 // site_step for both sites of pair p of an FP32 lattice with even nz, (x,y,z)
 // and (x,y,z+nz/2), in packed FP32 (f2): the same staples, projection, E
 // update and exponential per lane, at half the instructions.  SEAM: the pair
@@ -114,7 +118,7 @@ TCYM_HD typename F::Mat2 staple_sum_pair(const void *U, int64_t Vh, const PairNb
     using G2 = typename F::G2;
     using M2 = typename F::Mat2;
     M2 A = G2::zero();
-#pragma unroll
+#pragma unroll kPairStapleUnroll
     for (int k = 1; k <= 2; ++k) {
         const int nu = mu + k >= 3 ? mu + k - 3 : mu + k;
         M2 a1 = F::load2(U, Vh, nu, nb.at(mu, 1), SEAM && nb.swapped(mu, 1));
@@ -436,11 +440,12 @@ template <class F> TCYM_HD void site_set_zero(const Geom &g, void *U, void *E, i
 }
 
 // E^a_mu(x) = sigma N(0,1) (field stream); computed in FP64 and rounded.
-template <class F> TCYM_HD void site_gaussian_efield(const Geom &g, void *E, double sigma, uint64_t seed, int64_t s) {
+template <class F>
+TCYM_HD void site_gaussian_efield(const Geom &g, void *E, double sigma, uint64_t seed, int64_t s, uint64_t step = 0) {
     using T = typename F::T;
     for (int mu = 0; mu < 3; ++mu) {
         double z[F::NA];
-        normals<double, F::NA>(seed, STREAM_EFIELD, 0, (uint32_t)s, (uint32_t)mu, z);
+        normals<double, F::NA>(seed, STREAM_EFIELD, step, (uint32_t)s, (uint32_t)mu, z);
         T e[F::NA];
         for (int a = 0; a < F::NA; ++a) e[a] = (T)(sigma * z[a]);
         F::store_e(E, g.V, mu, s, e);
