@@ -136,6 +136,30 @@ int tcym_gaussian_efield(tcym_lattice lat, double sigma, uint64_t seed);
  * T00, TXX, TYY, TZZ, ELECTRIC, MAGNETIC, the reference's ThermalEnergy line. */
 int tcym_thermalize(tcym_lattice lat, double beta, uint64_t seed, int rounds, double max_time, double dt,
                     double restore_tol, int every, double *series, int series_cap, int *records);
+
+/* ---------------------------------------------------- cooled Chern-Simons number
+ * ChernSimonsNumber::CoolingMethod (TOPOLOGY/CoolingMethod.cpp) at blocking level 0,
+ * the level of its real-time measurement (SphaleronSimulation.cpp:230-236).  The
+ * object holds the last two cooled copies UOld, UNew of the lattice's links; a copy
+ * is made as Cooling::CoolNSave does (GRADIENTFLOW/Cooling.cpp:156-175): max_steps
+ * GradientFlow::StandardUpdate steps of dtau = sqrt_dctau^2 from E = 0 (the
+ * reference: 128 steps, SphaleronSimulation.cpp:230).  The lattice is only read. */
+typedef struct tcym_cooling_s *tcym_cooling;
+int tcym_cooling_create(tcym_lattice lat, int max_steps, double sqrt_dctau, tcym_cooling *out);
+int tcym_cooling_destroy(tcym_cooling c);
+/* CoolingMethod::Start (:124-135): UNew = the cooled links, UOld = UNew. */
+int tcym_cooling_start(tcym_cooling c);
+/* CoolingMethod::Update(measure) (:141-166): UNew = the cooled links; if measure,
+ * delta = GetDeltaNCs(1) on the geodesic UOld -> UNew is added to the running total
+ * (DeltaNCsCoolRealTime) and returned in *delta (nullable); then UOld = UNew.
+ * TCYM_ERR_STATE before tcym_cooling_start. */
+int tcym_cooling_update(tcym_cooling c, int measure, double *delta);
+/* CoolingMethod::GetDeltaNCs(norder) (:77-120) on the current UOld, UNew: Simpson's
+ * rule along the geodesic EMid = -i Log(UNew UOld^dag), UMid(x) = exp(-i x EMid) UOld
+ * (SUNc/AdvancedOperations.cpp:432-442) of NCsDot = improved E.B / (8 pi^2). */
+int tcym_cooling_delta_ncs(tcym_cooling c, int norder, double *out);
+/* the sum of the measured updates (ChernSimonsNumber::DeltaNCsCoolRealTime) */
+int tcym_cooling_total(tcym_cooling c, double *out);
 /* U_mu(x) = exp(i t^a theta^a), theta^a = sigma * N(0,1) from the Philox link stream. */
 int tcym_random_links(tcym_lattice lat, double sigma, uint64_t seed);
 /* GaussLawRestoration::Restore (GAUSSLAWFIXING/GaussRestore.cpp:131-167): iterate

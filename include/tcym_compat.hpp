@@ -477,6 +477,43 @@ inline void CoolNSave(std::string, DOUBLE MaxCoolingSteps, INT MaxBlockingNumber
 }
 }  // namespace Cooling
 
+namespace ChernSimonsNumber {
+inline DOUBLE DeltaNCsCoolRealTime = 0.0;
+// CoolingMethod (TOPOLOGY/CoolingMethod.cpp) on GLinks::U at blocking level 0, its
+// real-time measurement level (SphaleronSimulation.cpp:236); the cooled copies live
+// on the device (tcym_cooling_*), flowed with GradientFlow::SqrtDcTauOverSpacing.
+namespace CoolingMethod {
+inline INT StandardBlockingLevel = 0;
+inline INT StandardCoolingMaxSteps = 128;
+inline tcym_cooling state = nullptr;
+// Init (:19-32)
+inline void Init() {
+    if (StandardBlockingLevel != 0)
+        throw std::invalid_argument("tcym: cooled N_CS with lattice blocking is not supported");
+    if (state) tcym_cooling_destroy(state);
+    tcym_compat::check(tcym_cooling_create(tcym_compat::bind(GLinks::U, EFields::E), (int)StandardCoolingMaxSteps,
+                                           GradientFlow::SqrtDcTauOverSpacing, &state),
+                       "cooling init");
+}
+// Start (:124-135)
+inline void Start() { tcym_compat::check(tcym_cooling_start(state), "cooling start"); }
+// Update(Measure) (:141-166): DeltaNCsCoolRealTime += GetDeltaNCs(1) when measuring
+inline void Update(INT Measure) {
+    tcym_compat::bind(GLinks::U, EFields::E);  // the host mirror, if dirty, to the device first
+    double d = 0.0;
+    tcym_compat::check(tcym_cooling_update(state, (int)Measure, &d), "cooling update");
+    DeltaNCsCooling = 0.0;
+    if (Measure == 1) DeltaNCsCoolRealTime += d;
+}
+// GetDeltaNCs(NOrder) (:77-120) on the current pair of cooled configurations
+inline DOUBLE GetDeltaNCs(INT NOrder) {
+    double d = 0.0;
+    tcym_compat::check(tcym_cooling_delta_ncs(state, (int)NOrder, &d), "cooled delta N_CS");
+    return d;
+}
+}  // namespace CoolingMethod
+}  // namespace ChernSimonsNumber
+
 namespace Observables {
 namespace Bulk {
 inline DOUBLE ESqr[3], BSqr[3];

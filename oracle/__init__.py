@@ -87,6 +87,11 @@ class Port:
         f("thermalize").argtypes = [_int_p, _dbl_p, _dbl_p, ctypes.c_double, ctypes.c_uint64, ctypes.c_int,
                                     ctypes.c_double, ctypes.c_double, ctypes.c_int, _dbl_p, ctypes.c_int]
         f("thermalize").restype = ctypes.c_int
+        f("ilog").argtypes = [ctypes.c_double, _dbl_p, _dbl_p]
+        f("cool").argtypes = [_int_p, _dbl_p, ctypes.c_double, ctypes.c_int]
+        f("geodesic").argtypes = [_int_p, _dbl_p, _dbl_p, ctypes.c_double, _dbl_p, _dbl_p]
+        f("cooled_delta_ncs").argtypes = [_int_p, _dbl_p, _dbl_p, ctypes.c_int]
+        f("cooled_delta_ncs").restype = ctypes.c_double
         f("random_links").argtypes = [_int_p, _dbl_p, ctypes.c_double, ctypes.c_uint64]
         f("matrix_iexp").argtypes = [ctypes.c_double, _dbl_p, _dbl_p]
         f("retr_igen").argtypes = [_dbl_p, _dbl_p]
@@ -148,6 +153,23 @@ class Port:
         n = self._f("thermalize")(_n(shape), _p(U), _p(E), beta, seed, rounds, max_time, dt, every, _p(series), cap)
         return series[:n].copy()
 
+    def ilog(self, c, v):
+        """A with exp(i c A^a t^a) = v (MatrixILog, principal branch)."""
+        out = np.zeros(NA[self.nc])
+        self._f("ilog")(c, _p(np.ascontiguousarray(v, dtype=np.float64)), _p(out))
+        return out
+
+    def cool(self, shape, U, sqrt_dctau, nsteps):
+        self._f("cool")(_n(shape), _p(U), sqrt_dctau, nsteps)
+
+    def geodesic(self, shape, Uold, Unew, c):
+        Um, Em = empty_fields(self.nc, shape)
+        self._f("geodesic")(_n(shape), _p(Uold), _p(Unew), c, _p(Um), _p(Em))
+        return Um, Em
+
+    def cooled_delta_ncs(self, shape, Uold, Unew, norder=1):
+        return self._f("cooled_delta_ncs")(_n(shape), _p(Uold), _p(Unew), norder)
+
     def random_links(self, shape, U, sigma, seed):
         self._f("random_links")(_n(shape), _p(U), sigma, seed)
 
@@ -207,6 +229,11 @@ class Ref:
         L.ref_flow.argtypes = [ctypes.c_double, ctypes.c_int, ctypes.c_int]
         L.ref_flow.restype = ctypes.c_double
         L.ref_thermal_efield.argtypes = [ctypes.c_double, ctypes.c_uint64]
+        L.ref_cooling_init.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double]
+        L.ref_cooling_update.argtypes = [ctypes.c_int]
+        L.ref_cooling_update.restype = ctypes.c_double
+        L.ref_cooling_links.argtypes = [_dbl_p]
+        L.ref_matrix_ilog.argtypes = [ctypes.c_double, _dbl_p, _dbl_p]
         L.ref_thermalize.argtypes = [ctypes.c_double, ctypes.c_uint64, ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                      ctypes.c_char_p]
         L.ref_observables.argtypes = [_dbl_p]
@@ -255,6 +282,25 @@ class Ref:
     def observables(self):
         out = np.zeros(16)
         self.lib.ref_observables(_p(out))
+        return out
+
+    def cooling_init(self, blocking, max_steps, block_frequency, sqrt_dctau):
+        self.lib.ref_cooling_init(blocking, max_steps, block_frequency, sqrt_dctau)
+
+    def cooling_start(self):
+        self.lib.ref_cooling_start()
+
+    def cooling_update(self, measure):
+        return self.lib.ref_cooling_update(measure)
+
+    def cooling_links(self):
+        U, _ = empty_fields(self.nc, self.shape)
+        self.lib.ref_cooling_links(_p(U))
+        return U
+
+    def matrix_ilog(self, c, v):
+        out = np.zeros(NA[self.nc])
+        self.lib.ref_matrix_ilog(c, _p(np.ascontiguousarray(v, dtype=np.float64)), _p(out))
         return out
 
     def thermalize(self, beta, seed, rounds, max_time, dtau, outdir):

@@ -200,4 +200,51 @@ static inline double su3_unitarity_norm(const cplx *v) {
     return sqrt(n);
 }
 
+
+/* ---------------------------------------------------------------- matrix logs
+ * A^a with exp(i c A^a t^a) = V for a group element V and c = +-1 (the
+ * reference calls it with c = -1, SUNc/AdvancedOperations.cpp:432-442), using
+ * the principal logarithm: eigenphases in (-pi, pi].
+ *   SU(2) (MatrixILog, SU2/AlgebraOperations.cpp:56-74): V = cos(t) + i sin(t) n.sigma,
+ *         t = atan2(|v|, v3), A = 2 t n / c.
+ *   SU(3) (MatrixILog, SU3/AlgebraOperations.cpp:186-233, there via LAPACK zgeev):
+ *         V is normal, so it shares its eigenvectors with the commuting Hermitian
+ *         matrices (V + V^dag)/2 and (V - V^dag)/(2i); they are found as those of
+ *         C = (V + V^dag)/2 + g (V - V^dag)/(2i), g = 0.6180339887 (eigenvalues
+ *         cos t + g sin t separate the pairs t, -t that share a cosine), and
+ *         H = W diag(arg(w_k^dag V w_k)) W^dag, A^a = 2 tr(t^a H) / c. */
+static inline void su2_ilog(double c, const double *v, double *out) {
+    double d = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+    if (d == 0.0) { out[0] = out[1] = out[2] = 0.0; return; }
+    double m = 2.0 * atan2(d, v[3]) / (c * d);
+    out[0] = m * v[0]; out[1] = m * v[1]; out[2] = m * v[2];
+}
+static inline void su3_ilog(double c, const cplx *v, double *out) {
+    const double g = 0.6180339887498949;
+    cplx h[9], wv[9];
+    double w[3];
+    for (int i = 0; i < 3; ++i)
+        for (int k = 0; k < 3; ++k) {
+            cplx a = v[M3(i, k)], b = conj(v[M3(k, i)]);
+            h[M3(i, k)] = 0.5 * (a + b) + g * (a - b) / (2.0 * I);
+        }
+    su3_hermitian_eigen(h, w, wv);
+    double th[3];
+    for (int j = 0; j < 3; ++j) {
+        cplx z = 0.0;  /* w_j^dag V w_j */
+        for (int i = 0; i < 3; ++i)
+            for (int k = 0; k < 3; ++k) z += conj(wv[M3(i, j)]) * v[M3(i, k)] * wv[M3(k, j)];
+        th[j] = atan2(cimag(z), creal(z));
+    }
+    cplx hm[9], t[8];
+    for (int i = 0; i < 3; ++i)
+        for (int k = 0; k < 3; ++k) {
+            cplx s = 0.0;
+            for (int j = 0; j < 3; ++j) s += wv[M3(i, j)] * th[j] * conj(wv[M3(k, j)]);
+            hm[M3(i, k)] = s;
+        }
+    su3_tr_gen(hm, t);
+    for (int a = 0; a < 8; ++a) out[a] = 2.0 * creal(t[a]) / c;
+}
+
 #endif

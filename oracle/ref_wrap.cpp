@@ -98,6 +98,9 @@ DOUBLE Qs = 1.0;
 #include "DYNAMICS/LangevinDynamics.cpp"
 #undef const
 #include "GRADIENTFLOW/GradientFlow.cpp"
+#include "TOPOLOGY/VacuumEstimator.cpp"
+#include "GRADIENTFLOW/Cooling.cpp"
+#include "TOPOLOGY/CoolingMethod.cpp"
 
 static bool g_langevin_ready = false;
 
@@ -200,6 +203,36 @@ void ref_thermalize(double beta, uint64_t seed, int rounds, double max_time, dou
     RandomNumberGenerator::MySEED = (long int)seed;
     RandomNumberGenerator::SetStream(seed, ORC_STREAM_EFIELD, 0);
     ThermalDynamics::Thermalize(rounds, max_time);
+}
+
+/* ChernSimonsNumber::CoolingMethod (TOPOLOGY/CoolingMethod.cpp): Init with the
+ * given standard blocking level, cooling steps, Cooling::BlockFrequency and flow
+ * step, then Start (:124-135) or Update(measure) (:141-166) on the current links;
+ * update returns ChernSimonsNumber::DeltaNCsCoolRealTime.  SU(3) measurements reach
+ * MatrixILog, i.e. the zgeev stub, and abort: SU(2) only for measure = 1. */
+void ref_cooling_init(int blocking, int max_steps, int block_frequency, double sqrt_dctau) {
+    ChernSimonsNumber::CoolingMethod::StandardBlockingLevel = blocking;
+    ChernSimonsNumber::CoolingMethod::StandardCoolingMaxSteps = max_steps;
+    Cooling::BlockFrequency = block_frequency;
+    GradientFlow::SqrtDcTauOverSpacing = sqrt_dctau;
+    ChernSimonsNumber::DeltaNCsCoolRealTime = 0.0;
+    ChernSimonsNumber::CoolingMethod::Init();
+}
+void ref_cooling_start() { ChernSimonsNumber::CoolingMethod::Start(); }
+double ref_cooling_update(int measure) {
+    ChernSimonsNumber::CoolingMethod::Update(measure);
+    return ChernSimonsNumber::DeltaNCsCoolRealTime;
+}
+/* the cooled links UOld (after Start/Update it equals UNew) */
+void ref_cooling_links(double *U) {
+    GaugeLinks *u = ChernSimonsNumber::CoolingMethod::UOld;
+    std::memcpy(U, u->U, sizeof(SU_Nc_FUNDAMENTAL_FORMAT) * 3 * SUNcGroup::MatrixSize * u->Volume);
+}
+/* SUNcAlgebra::Operations::MatrixILog (SU2/AlgebraOperations.cpp:56-74) */
+void ref_matrix_ilog(double c, const double *v, double *out) {
+    SU_Nc_FUNDAMENTAL_FORMAT m[SUNcGroup::MatrixSize];
+    std::memcpy(m, v, sizeof(m));
+    SUNcAlgebra::Operations::MatrixILog(c, m, out);
 }
 
 /* Observables: Bulk (OBSERVABLES/BulkObservables.cpp:133-143), GaussLaw

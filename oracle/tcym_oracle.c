@@ -45,6 +45,7 @@ double orc_normal_c(uint64_t seed, uint32_t stream, uint64_t step, uint32_t site
 #define G_ADJ su2_adjoint
 #define G_INVADJ su2_inverse_adjoint
 #define G_UNORM su2_unitarity_norm
+#define G_ILOG su2_ilog
 #include "orc_lattice.inc"
 #undef PFX
 #undef MAT
@@ -59,6 +60,7 @@ double orc_normal_c(uint64_t seed, uint32_t stream, uint64_t step, uint32_t site
 #undef G_ADJ
 #undef G_INVADJ
 #undef G_UNORM
+#undef G_ILOG
 #undef OFF
 
 /* ---- SU(3) instantiation ---- */
@@ -75,4 +77,5 @@ double orc_normal_c(uint64_t seed, uint32_t stream, uint64_t step, uint32_t site
 #define G_ADJ su3_adjoint
 #define G_INVADJ su3_inverse_adjoint
 #define G_UNORM su3_unitarity_norm
+#define G_ILOG su3_ilog
 #include "orc_lattice.inc"

@@ -35,6 +35,8 @@ def load():
         L.hc_reunitarize.argtypes = [ctypes.c_int, ip, _vp]
         L.hc_init.argtypes = [ctypes.c_int, ip, _vp, _vp, ctypes.c_int, ctypes.c_double, ctypes.c_uint64]
         L.hc_iexp.argtypes = [ctypes.c_int, ctypes.c_double, _vp, _vp]
+        L.hc_ilog.argtypes = [ctypes.c_int, ctypes.c_double, _vp, _vp]
+        L.hc_geodesic.argtypes = [ctypes.c_int, ip, _vp, _vp, ctypes.c_double, _vp, _vp]
         L.hc_normal.argtypes = [ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32,
                                 ctypes.c_uint32, ctypes.c_int]
         L.hc_normal.restype = ctypes.c_double
@@ -110,12 +112,24 @@ class HostLattice:
     def init(self, what, sigma=0.0, seed=0):
         self.L.hc_init(self.fmt, self.n, _p(self.U[self.cur]), _p(self.E), what, sigma, seed)
 
+    def geodesic(self, old, new, c):
+        """UMid, EMid (into this lattice) of the geodesic from old's links to new's."""
+        self.L.hc_geodesic(self.fmt, self.n, _p(old.U[old.cur]), _p(new.U[new.cur]), c, _p(self.U[self.cur]),
+                           _p(self.E))
+
 
 def iexp(nc, prec, c, alpha):
     L = load()
     out = np.zeros(NM[nc])
     a = np.ascontiguousarray(alpha, dtype=np.float64)
     L.hc_iexp(FMT[(nc, prec)], c, _p(a), _p(out))
+    return out
+
+
+def ilog(nc, prec, c, v):
+    L = load()
+    out = np.zeros(NA[nc])
+    L.hc_ilog(FMT[(nc, prec)], c, _p(np.ascontiguousarray(v, dtype=np.float64)), _p(out))
     return out
 
 

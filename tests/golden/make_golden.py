@@ -19,6 +19,13 @@ CUDA library draws); every output below is produced by the reference itself:
                            lattice from U = 1, beta 2, seed 7, dTau 0.0375 (20
                            steps a round): final U, E and the ThermalEnergy file
                            (every 20 steps; the reference writes 6 digits)
+  ref_cooling_su2.npz      ChernSimonsNumber::CoolingMethod, SU(2) (6,6,6): a
+                           random-link state (seed 3, sigma 0.5; E seed 4, 0.7,
+                           restored); Start, then 3 x (20 leapfrog steps at dt
+                           0.05, Update(1)) with 16 cooling steps of sqrt_dctau
+                           sqrt(0.02): the cumulative DeltaNCsCoolRealTime after
+                           each update and the cooled links (SU(3) measurements
+                           need LAPACK zgeev, absent here)
 
   python tests/golden/make_golden.py
 """
@@ -120,6 +127,26 @@ def thermalize(nc):
                         shape=np.array(shape), beta=2.0, seed=7, rounds=2, max_time=0.75, dtau=0.0375)
 
 
+def cooling():
+    P, R = oracle.Port(2), oracle.Ref(2)
+    shape = (6, 6, 6)
+    U, E = oracle.empty_fields(2, shape)
+    P.random_links(shape, U, 0.5, 3)
+    P.gaussian_efield(shape, E, 0.7, 4)
+    P.gauss_restore(shape, U, E, 1e-14, 10000)
+    R.init(shape)
+    R.set(U, E)
+    R.cooling_init(0, 16, 8, np.sqrt(0.02))
+    R.cooling_start()
+    totals, cooled = [], []
+    for _ in range(3):
+        R.leapfrog(0.05, 20)
+        totals.append(R.cooling_update(1))
+        cooled.append(R.cooling_links())
+    np.savez_compressed(os.path.join(HERE, "ref_cooling_su2.npz"), U0=U, E0=E, totals=np.array(totals),
+                        cooled=np.array(cooled), steps=16, sqrt_dctau=np.sqrt(0.02), dt=0.05, every=20)
+
+
 if __name__ == "__main__":
     oracle.build()
     if not (oracle.ref_available(2) and oracle.ref_available(3)):
@@ -130,6 +157,7 @@ if __name__ == "__main__":
     config0()
     for nc in (2, 3):
         thermalize(nc)
+    cooling()
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))

@@ -237,3 +237,42 @@ def test_thermalize_parity(ctx, oracle_port, nc, prec):
     assert np.abs(series - ref).max() <= tol * np.abs(ref).max()
     Ug, Eg = lat.download()
     assert rel(Ug, U) < tol and rel(Eg, E) < tol
+
+
+@pytest.mark.parametrize("prec", PREC)
+@pytest.mark.parametrize("nc", GROUPS)
+def test_cooled_delta_ncs_parity(ctx, oracle_port, nc, prec):
+    """tcym_cooling_* against the oracle's CoolingMethod: Start, then three rounds of
+    20 leapfrog steps and Update(1) with 16 cooling steps; the cumulative cooled
+    Delta N_CS after each update and GetDeltaNCs(2) on the last pair."""
+    shape = (6, 6, 6)
+    P = oracle_port[nc]
+    U, E = random_state(P, nc, shape, seed=3, sigma_u=0.5)
+    P.gauss_restore(shape, U, E, 1e-14, 10000)
+    lat = tcym.Lattice(ctx, nc, shape, prec)
+    lat.set_reunitarize_period(0)
+    lat.upload(U, E)
+    if prec == tcym.FP32:
+        U, E = lat.download()
+    s, steps = np.sqrt(0.02), 16
+    cool = tcym.Cooling(lat, steps, s)
+    cool.start()
+    old = U.copy()
+    P.cool(shape, old, s, steps)
+    total, scale = 0.0, 0.0
+    for _ in range(3):
+        lat.leapfrog(0.05, 20)
+        P.leapfrog(shape, U, E, 0.05, 20)
+        new = U.copy()
+        P.cool(shape, new, s, steps)
+        d = P.cooled_delta_ncs(shape, old, new, 1)
+        total += d
+        scale = max(scale, abs(d))
+        got = cool.update(True)
+        tol = 1e-9 if prec == tcym.FP64 else 1e-3
+        assert abs(got - d) <= tol * max(scale, 1e-3), (got, d)
+        assert abs(cool.total() - total) <= 3 * tol * max(scale, 1e-3)
+        old = new
+    ref2 = P.cooled_delta_ncs(shape, old, new, 2)
+    assert abs(cool.delta_ncs(2) - ref2) <= (1e-9 if prec == tcym.FP64 else 1e-3) * max(abs(ref2), 1e-3)
+    cool.close()

@@ -138,3 +138,25 @@ def test_thermalize_equals_reference(oracle_port, nc):
     assert series.shape == d["series"].shape
     assert np.allclose(series, d["series"], rtol=5e-6, atol=1e-6)
     assert rel(U, d["U"]) < 1e-12 and rel(E, d["E"]) < 1e-12
+
+
+def test_cooled_delta_ncs_equals_reference(oracle_port):
+    """ChernSimonsNumber::CoolingMethod (SU(2), where the reference's matrix log needs
+    no LAPACK): the oracle's cooling, geodesic and Simpson rule reproduce the
+    reference's cumulative cooled Delta N_CS and its cooled links."""
+    d = load("ref_cooling_su2.npz")
+    P = oracle_port[2]
+    shape = (6, 6, 6)
+    U, E = d["U0"].copy(), d["E0"].copy()
+    steps, s = int(d["steps"]), float(d["sqrt_dctau"])
+    old = U.copy()
+    P.cool(shape, old, s, steps)
+    total = 0.0
+    for k in range(3):
+        P.leapfrog(shape, U, E, float(d["dt"]), int(d["every"]))
+        new = U.copy()
+        P.cool(shape, new, s, steps)
+        total += P.cooled_delta_ncs(shape, old, new, 1)
+        assert abs(total - d["totals"][k]) < 1e-12, (k, total, d["totals"][k])
+        assert rel(new, d["cooled"][k]) < 1e-12
+        old = new

@@ -177,3 +177,47 @@ def test_initial_conditions(oracle_port, nc):
     H.init(1, 0.5, 1)
     Uh, Eh = H.download()
     assert rel(Eh, E) < 1e-15 and rel(Uh, U) < 1e-13
+
+
+@pytest.mark.parametrize("nc", [2, 3])
+def test_matrix_log(oracle_port, nc):
+    """The device matrix log (host build, FP64) against the oracle's, and exp(log V) = V:
+    generic elements, small rotations (the geodesic's case), the identity, elements
+    with degenerate eigenvalues, and rotations near the branch cut (eigenphases ~ pi)."""
+    P = oracle_port[nc]
+    rng = np.random.default_rng(8)
+    na = 3 if nc == 2 else 8
+    cases = [rng.normal(size=na) * s for s in (1e-6, 0.05, 0.5, 1.5) for _ in range(4)]
+    cases.append(np.zeros(na))
+    if nc == 3:
+        cases += [np.array([0, 0, 1.2, 0, 0, 0, 0, 0.0]), np.array([0, 0, 0, 0, 0, 0, 0, 2.0]),
+                  np.array([0, 0, 0.9, 0, 0, 0, 0, 0.9 / np.sqrt(3)])]  # two equal eigenphases
+    else:
+        cases += [np.array([0, 0, 2 * np.pi - 1e-3])]
+    for a in cases:
+        v = P.matrix_iexp(-1.0, a)
+        got, ref = hc.ilog(nc, "f64", -1.0, v), P.ilog(-1.0, v)
+        assert np.abs(got - ref).max() < 1e-9 * max(1.0, np.abs(ref).max()), (a, got, ref)
+        assert np.abs(P.matrix_iexp(-1.0, got) - v).max() < 1e-12
+
+
+@pytest.mark.parametrize("nc,prec", FORMATS)
+def test_site_geodesic(oracle_port, nc, prec):
+    """GeodesicInterpolation on every link: UMid and EMid against the oracle."""
+    P = oracle_port[nc]
+    shape = (4, 4, 6)
+    Uo, _ = oracle.empty_fields(nc, shape)
+    Un, _ = oracle.empty_fields(nc, shape)
+    P.random_links(shape, Uo, 0.4, 12)
+    P.random_links(shape, Un, 0.4, 13)
+    A, B, M = (hc.HostLattice(nc, prec, shape) for _ in range(3))
+    A.upload(Uo, None)
+    B.upload(Un, None)
+    if prec == "f32":  # the oracle starts from the rounded links
+        Uo, Un = A.download()[0], B.download()[0]
+    for c in (0.0, 0.5, 1.0):
+        M.geodesic(A, B, c)
+        Um, Em = P.geodesic(shape, Uo, Un, c)
+        Uh, Eh = M.download()
+        assert rel(Uh, Um) < TOL[prec] and rel(Eh, Em) < TOL[prec]
+    assert rel(M.download()[0], Un) < TOL[prec]  # c = 1 lands on UNew

@@ -119,6 +119,12 @@ def library() -> ctypes.CDLL:
         "tcym_lattice_stream": ([ctypes.c_void_p, c_void_pp], ctypes.c_int),
         "tcym_set_zero": ([ctypes.c_void_p], ctypes.c_int),
         "tcym_gaussian_efield": ([ctypes.c_void_p, ctypes.c_double, ctypes.c_uint64], ctypes.c_int),
+        "tcym_cooling_create": ([ctypes.c_void_p, ctypes.c_int, ctypes.c_double, c_void_pp], ctypes.c_int),
+        "tcym_cooling_destroy": ([ctypes.c_void_p], ctypes.c_int),
+        "tcym_cooling_start": ([ctypes.c_void_p], ctypes.c_int),
+        "tcym_cooling_update": ([ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double)], ctypes.c_int),
+        "tcym_cooling_delta_ncs": ([ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double)], ctypes.c_int),
+        "tcym_cooling_total": ([ctypes.c_void_p, ctypes.POINTER(ctypes.c_double)], ctypes.c_int),
         "tcym_thermalize": ([ctypes.c_void_p, ctypes.c_double, ctypes.c_uint64, ctypes.c_int, ctypes.c_double,
                              ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
                              ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
@@ -340,6 +346,46 @@ class Lattice:
 
     def ncs_reset(self):
         self.ctx.check(self.lib.tcym_ncs_reset(self.h))
+
+
+class Cooling:
+    """ChernSimonsNumber::CoolingMethod at blocking level 0 (tcym_cooling_*): cooled
+    copies of a lattice's links and the cooled real-time Delta N_CS between them."""
+
+    def __init__(self, lat: "Lattice", max_steps: int = 128, sqrt_dctau: float = 0.125 ** 0.5):
+        self.lat, self.ctx, self.lib = lat, lat.ctx, lat.lib
+        h = ctypes.c_void_p()
+        self.ctx.check(self.lib.tcym_cooling_create(lat.h, max_steps, sqrt_dctau, ctypes.byref(h)))
+        self.h = h
+
+    def start(self):
+        self.ctx.check(self.lib.tcym_cooling_start(self.h))
+
+    def update(self, measure: bool = True) -> float:
+        d = ctypes.c_double()
+        self.ctx.check(self.lib.tcym_cooling_update(self.h, int(measure), ctypes.byref(d)))
+        return d.value
+
+    def delta_ncs(self, norder: int = 1) -> float:
+        d = ctypes.c_double()
+        self.ctx.check(self.lib.tcym_cooling_delta_ncs(self.h, norder, ctypes.byref(d)))
+        return d.value
+
+    def total(self) -> float:
+        d = ctypes.c_double()
+        self.ctx.check(self.lib.tcym_cooling_total(self.h, ctypes.byref(d)))
+        return d.value
+
+    def close(self):
+        if self.h:
+            self.lib.tcym_cooling_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 DYN_LEAPFROG, DYN_LANGEVIN = 0, 1

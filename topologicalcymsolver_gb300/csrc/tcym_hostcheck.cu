@@ -116,6 +116,22 @@ template <int FMT> struct H {
                 }
         }
     }
+    // A with exp(i c A^a t^a) = V, V given in the reference AoS link layout
+    static void ilog_aos(double c, const double *v, double *out) {
+        typename F::G::Mat m;
+        if constexpr (F::NA == 3) {
+            for (int k = 0; k < 4; ++k) m.q[k] = (T)v[k];
+        } else {
+            for (int i = 0; i < 3; ++i)
+                for (int j = 0; j < 3; ++j) m.m[i][j] = cx<T>{(T)v[2 * (i + 3 * j)], (T)v[2 * (i + 3 * j) + 1]};
+        }
+        T o[F::NA];
+        F::G::ilog((T)c, m, o);
+        for (int a = 0; a < F::NA; ++a) out[a] = (double)o[a];
+    }
+    static void geodesic(const Geom &g, const void *Uold, const void *Unew, double c, void *Umid, void *Emid) {
+        for (int64_t s = 0; s < g.V; ++s) site_geodesic<F>(g, Uold, Unew, c, Umid, Emid, s);
+    }
     static int gauss_restore(const Geom &g, const void *U, void *E, double tol, int maxit) {
         std::vector<double> G((size_t)F::NA * g.V);
         const double gam[3] = {7.0 / 24.0, 7.0 / 48.0, 7.0 / 72.0};
@@ -202,6 +218,15 @@ int hc_init(int fmt, const int *n, void *U, void *E, int what, double sigma, uin
         else if (what == 1) site_gaussian_efield<HH::F>(g, E, sigma, seed, s);
         else site_random_links<HH::F>(g, U, sigma, seed, s);
     });
+    return 0;
+}
+int hc_ilog(int fmt, double c, const double *v, double *out) {
+    HC_DISPATCH(fmt, HH::ilog_aos(c, v, out));
+    return 0;
+}
+int hc_geodesic(int fmt, const int *n, const void *Uold, const void *Unew, double c, void *Umid, void *Emid) {
+    Geom g = geom(n);
+    HC_DISPATCH(fmt, HH::geodesic(g, Uold, Unew, c, Umid, Emid));
     return 0;
 }
 // exp(i c t^a alpha^a) in the format's precision, returned in the reference AoS link layout

@@ -220,6 +220,11 @@ template <int FMT> __global__ void k_reunitarize(Geom g, void *U) {
     int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (s < g.V) site_reunitarize<Fmt<FMT>>(g, U, s);
 }
+template <int FMT>
+__global__ void k_geodesic(Geom g, const void *Uold, const void *Unew, double c, void *Umid, void *Emid) {
+    int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < g.V) site_geodesic<Fmt<FMT>>(g, Uold, Unew, c, Umid, Emid, s);
+}
 template <int FMT> __global__ void k_from_aos(Geom g, void *U, void *E, const double *Ua, const double *Ea) {
     int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (s < g.V) site_from_aos<Fmt<FMT>>(g, U, E, Ua, Ea, s);
@@ -287,6 +292,11 @@ template <int FMT> struct Launch {
     }
     static cudaError_t random_links(const Geom &g, void *U, double sigma, uint64_t seed, cudaStream_t st) {
         k_random_links<FMT><<<grid_for(g.V, 128), 128, 0, st>>>(g, U, sigma, seed);
+        return cudaGetLastError();
+    }
+    static cudaError_t geodesic(const Geom &g, const void *Uold, const void *Unew, double c, void *Umid, void *Emid,
+                                cudaStream_t st) {
+        k_geodesic<FMT><<<grid_for(g.V, 128), 128, 0, st>>>(g, Uold, Unew, c, Umid, Emid);
         return cudaGetLastError();
     }
     static cudaError_t reunitarize(const Geom &g, void *U, cudaStream_t st) {

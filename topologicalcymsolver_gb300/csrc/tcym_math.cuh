@@ -237,6 +237,13 @@ template <class T> struct SU2 {
         T n = Real<T>::rsqrt_(v.q[0] * v.q[0] + v.q[1] * v.q[1] + v.q[2] * v.q[2] + v.q[3] * v.q[3]);
         return scale(n, v);
     }
+    // A^a with exp(i c A^a t^a) = V, c = +-1, principal branch (MatrixILog,
+    // SU2/AlgebraOperations.cpp:56-74): V = cos t + i sin t n.sigma, A = 2 t n / c
+    static TCYM_HD void ilog(T c, const Mat &v, T *out) {
+        const T d = Real<T>::sqrt_(v.q[0] * v.q[0] + v.q[1] * v.q[1] + v.q[2] * v.q[2]);
+        const T m = d == T(0) ? T(0) : T(2) * atan2(d, v.q[3]) / (c * d);
+        out[0] = m * v.q[0]; out[1] = m * v.q[1]; out[2] = m * v.q[2];
+    }
 };
 
 // ------------------------------------------------------------------ SU(3)
@@ -588,6 +595,82 @@ template <class T> struct SU3 {
     static TCYM_HD cx<T> conj_cross(cx<T> x, cx<T> y, cx<T> z, cx<T> w) {
         return {fma(x.re, y.re, fma(-x.im, y.im, fma(-z.re, w.re, z.im * w.im))),
                 fma(z.re, w.im, fma(z.im, w.re, fma(-x.re, y.im, -(x.im * y.re))))};
+    }
+    // Hermitian A = W diag(w) W^dagger by cyclic complex Jacobi rotations (the
+    // rotation from tan t = sgn(tau) / (|tau| + sqrt(1 + tau^2)), no trigonometry),
+    // at most 30 sweeps.
+    static TCYM_HD void hermitian_eigen(Mat a, T *w, Mat &W) {
+        W = identity();
+        for (int sweep = 0; sweep < 30; ++sweep) {
+            const T off = abs2(a.m[0][1]) + abs2(a.m[0][2]) + abs2(a.m[1][2]);
+            const T diag = a.m[0][0].re * a.m[0][0].re + a.m[1][1].re * a.m[1][1].re + a.m[2][2].re * a.m[2][2].re;
+            if (!(off > T(1e-32) * (diag + off))) break;
+            for (int p = 0; p < 2; ++p)
+                for (int q = p + 1; q < 3; ++q) {
+                    const cx<T> apq = a.m[p][q];
+                    const T r = Real<T>::sqrt_(abs2(apq));
+                    if (r == T(0)) continue;
+                    const cx<T> ph{apq.re / r, apq.im / r};  // a_pq = r e^{i phi}
+                    const T tau = (a.m[q][q].re - a.m[p][p].re) / (T(2) * r);
+                    const T t = (tau >= T(0) ? T(1) : T(-1)) / (fabs(tau) + Real<T>::sqrt_(T(1) + tau * tau));
+                    const T cs = T(1) / Real<T>::sqrt_(T(1) + t * t), sn = t * cs;
+                    // columns p, q of A and W: col_p' = c col_p - s conj(ph) col_q, col_q' = s ph col_p + c col_q
+                    const cx<T> gqp{-sn * ph.re, sn * ph.im}, gpq{sn * ph.re, sn * ph.im};
+                    for (int k = 0; k < 3; ++k) {
+                        const cx<T> akp = a.m[k][p], akq = a.m[k][q], wkp = W.m[k][p], wkq = W.m[k][q];
+                        a.m[k][p] = cx<T>{cs * akp.re, cs * akp.im} + akq * gqp;
+                        a.m[k][q] = akp * gpq + cx<T>{cs * akq.re, cs * akq.im};
+                        W.m[k][p] = cx<T>{cs * wkp.re, cs * wkp.im} + wkq * gqp;
+                        W.m[k][q] = wkp * gpq + cx<T>{cs * wkq.re, cs * wkq.im};
+                    }
+                    for (int k = 0; k < 3; ++k) {  // rows: A <- G^dagger A
+                        const cx<T> apk = a.m[p][k], aqk = a.m[q][k];
+                        a.m[p][k] = cx<T>{cs * apk.re, cs * apk.im} + conj(gqp) * aqk;
+                        a.m[q][k] = conj(gpq) * apk + cx<T>{cs * aqk.re, cs * aqk.im};
+                    }
+                }
+        }
+        w[0] = a.m[0][0].re; w[1] = a.m[1][1].re; w[2] = a.m[2][2].re;
+    }
+    static TCYM_HD T abs2(cx<T> z) { return z.re * z.re + z.im * z.im; }
+    // A^a with exp(i c A^a t^a) = V, c = +-1, principal branch (MatrixILog,
+    // SU3/AlgebraOperations.cpp:186-233, there through LAPACK zgeev): the normal V
+    // shares its eigenvectors with the commuting Hermitian (V + V^dag)/2 and
+    // (V - V^dag)/(2i), found as those of C = (V + V^dag)/2 + g (V - V^dag)/(2i),
+    // g = 0.618... (eigenvalues cos t + g sin t keep t and -t apart);
+    // H = W diag(arg(w_k^dag V w_k)) W^dag and A^a = 2 tr(t^a H) / c.
+    static TCYM_HD void ilog(T c, const Mat &v, T *out) {
+        const T g = T(0.6180339887498949);
+        Mat h;
+        for (int i = 0; i < 3; ++i)
+            for (int k = 0; k < 3; ++k) {
+                const cx<T> a = v.m[i][k], b = conj(v.m[k][i]);
+                // (a + b)/2 + g (a - b)/(2i) = (a + b)/2 - i g (a - b)/2
+                h.m[i][k] = cx<T>{T(0.5) * (a.re + b.re) + T(0.5) * g * (a.im - b.im),
+                                  T(0.5) * (a.im + b.im) - T(0.5) * g * (a.re - b.re)};
+            }
+        T w[3];
+        Mat W;
+        hermitian_eigen(h, w, W);
+        T th[3];
+        for (int j = 0; j < 3; ++j) {
+            cx<T> z{T(0), T(0)};  // w_j^dag V w_j
+            for (int i = 0; i < 3; ++i) {
+                cx<T> vw{T(0), T(0)};
+                for (int k = 0; k < 3; ++k) vw = cfma(v.m[i][k], W.m[k][j], vw);
+                z = cfma_cn(W.m[i][j], vw, z);
+            }
+            th[j] = atan2(z.im, z.re);
+        }
+        Mat hm;  // H = W diag(th) W^dagger (Hermitian)
+        for (int i = 0; i < 3; ++i)
+            for (int k = 0; k < 3; ++k) {
+                cx<T> s{T(0), T(0)};
+                for (int j = 0; j < 3; ++j) s = cfma_nc(cx<T>{th[j] * W.m[i][j].re, th[j] * W.m[i][j].im}, W.m[k][j], s);
+                hm.m[i][k] = s;
+            }
+        algebra_components(hm, out);
+        for (int a = 0; a < NA; ++a) out[a] = out[a] / c;
     }
     // Gram-Schmidt of rows 0 and 1, row 2 rebuilt: the nearest SU(3) matrix
     // for a link that has drifted by rounding (not a max-trace projection).

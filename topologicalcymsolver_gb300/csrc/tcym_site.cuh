@@ -453,47 +453,55 @@ TCYM_HD void site_gaussian_efield(const Geom &g, void *E, double sigma, uint64_t
 }
 
 // U_mu(x) = exp(i t^a theta^a), theta^a = sigma N(0,1) (link stream); FP64 then rounded.
+// a link in another precision
+template <class T, class S> TCYM_HD Q4<T> recast(const Q4<S> &m) {
+    return Q4<T>{{(T)m.q[0], (T)m.q[1], (T)m.q[2], (T)m.q[3]}};
+}
+template <class T, class S> TCYM_HD M3<T> recast(const M3<S> &m) {
+    M3<T> r;
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) r.m[i][j] = cx<T>{(T)m.m[i][j].re, (T)m.m[i][j].im};
+    return r;
+}
+template <class F> using Group64 = typename std::conditional<F::NA == 3, SU2<double>, SU3<double>>::type;
+
 template <class F> TCYM_HD void site_random_links(const Geom &g, void *U, double sigma, uint64_t seed, int64_t s) {
-    using G64 = typename std::conditional<F::NA == 3, SU2<double>, SU3<double>>::type;
+    using G64 = Group64<F>;
     using T = typename F::T;
     for (int mu = 0; mu < 3; ++mu) {
         double th[F::NA];
         normals<double, F::NA>(seed, STREAM_LINKS, 0, (uint32_t)s, (uint32_t)mu, th);
         for (int a = 0; a < F::NA; ++a) th[a] *= sigma;
-        typename G64::Mat m = G64::iexp(1.0, th);
-        typename F::Mat r;
-        if constexpr (F::NA == 3) {
-            for (int k = 0; k < 4; ++k) r.q[k] = (T)m.q[k];
-        } else {
-            for (int i = 0; i < 3; ++i)
-                for (int j = 0; j < 3; ++j) r.m[i][j] = cx<T>{(T)m.m[i][j].re, (T)m.m[i][j].im};
-        }
-        F::store(U, g.V, mu, s, r);
+        F::store(U, g.V, mu, s, recast<T>(G64::iexp(1.0, th)));
     }
 }
 
 // FP64 reunitarisation of the stored links (new: the reference only monitors
 // unitarity).  Links are widened to FP64, projected and rounded back.
 template <class F> TCYM_HD void site_reunitarize(const Geom &g, void *U, int64_t s) {
-    using G64 = typename std::conditional<F::NA == 3, SU2<double>, SU3<double>>::type;
+    using T = typename F::T;
+    for (int mu = 0; mu < 3; ++mu)
+        F::store(U, g.V, mu, s, recast<T>(Group64<F>::reunitarize(recast<double>(F::load(U, g.V, mu, s)))));
+}
+
+// GeodesicInterpolation (SUNc/AdvancedOperations.cpp:432-442) on the links of
+// site s, in FP64 whatever the storage: EMid = ILog(-1, UNew UOld^dag) and
+// UMid = IExp(-c, EMid) UOld, so UMid runs from UOld (c = 0) to UNew (c = 1);
+// EMid in field units (CoolingMethod.cpp:39-70: cE = 1 at unit spacing).
+template <class F>
+TCYM_HD void site_geodesic(const Geom &g, const void *Uold, const void *Unew, double c, void *Umid, void *Emid,
+                           int64_t s) {
+    using G64 = Group64<F>;
     using T = typename F::T;
     for (int mu = 0; mu < 3; ++mu) {
-        typename F::Mat m = F::load(U, g.V, mu, s);
-        typename G64::Mat d;
-        if constexpr (F::NA == 3) {
-            for (int k = 0; k < 4; ++k) d.q[k] = (double)m.q[k];
-        } else {
-            for (int i = 0; i < 3; ++i)
-                for (int j = 0; j < 3; ++j) d.m[i][j] = cx<double>{(double)m.m[i][j].re, (double)m.m[i][j].im};
-        }
-        d = G64::reunitarize(d);
-        if constexpr (F::NA == 3) {
-            for (int k = 0; k < 4; ++k) m.q[k] = (T)d.q[k];
-        } else {
-            for (int i = 0; i < 3; ++i)
-                for (int j = 0; j < 3; ++j) m.m[i][j] = cx<T>{(T)d.m[i][j].re, (T)d.m[i][j].im};
-        }
-        F::store(U, g.V, mu, s, m);
+        const typename G64::Mat uo = recast<double>(F::load(Uold, g.V, mu, s));
+        const typename G64::Mat un = recast<double>(F::load(Unew, g.V, mu, s));
+        double e[F::NA];
+        G64::ilog(-1.0, G64::template mulx<false, true>(un, uo), e);
+        F::store(Umid, g.V, mu, s, recast<T>(G64::mul(G64::iexp(-c, e), uo)));
+        T et[F::NA];
+        for (int a = 0; a < F::NA; ++a) et[a] = (T)e[a];
+        F::store_e(Emid, g.V, mu, s, et);
     }
 }
 
