@@ -275,7 +275,8 @@ def run_ours(a):
     traffic = ncu_traffic()
     roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
             "frac": round(achieved / peak, 4), "traffic": traffic,
-            "kernel": "k_step<SU3 FP32 two-row> (fused E and link update)",
+            "kernel": ("k_step_pair<SU3 FP32> (site pairs in packed FP32; fused E and link update)" if L % 2 == 0
+                       else "k_step<SU3 FP32> (fused E and link update)"),
             "bytes_per_link_update": BYTES_PER_LINK, "median_launch_ms": round(med * 1e3, 4),
             "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind}
 

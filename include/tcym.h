@@ -160,6 +160,22 @@ int tcym_cooling_update(tcym_cooling c, int measure, double *delta);
 int tcym_cooling_delta_ncs(tcym_cooling c, int norder, double *out);
 /* the sum of the measured updates (ChernSimonsNumber::DeltaNCsCoolRealTime) */
 int tcym_cooling_total(tcym_cooling c, double *out);
+
+/* ------------------------------------------------------- configuration files
+ * The reference's text format (IO/SaveConfiguration.cpp:3-56, IO/LoadConfiguration.cpp:3-120):
+ * a link file with one line "x y z mu v_0 .. v_{n-1} " per link (SU(2): 4 reals; SU(3):
+ * re, im of the 9 entries in storage order) and a field file with one line
+ * "x y z mu e^0 .. e^{NA-1}" per link, z-, y-, x-, mu-major, 15 significant digits.
+ * Host arrays in the reference AoS layouts (as tcym_lattice_upload).  Either file may be
+ * NULL.  Reading accepts lines in any order but needs every link exactly once
+ * (TCYM_ERR_ARG otherwise, with the reason on stderr; the reference exits instead). */
+int tcym_write_configuration(int nc, int nx, int ny, int nz, const double *U_aos, const double *E_aos,
+                             const char *ufile, const char *efile);
+int tcym_read_configuration(int nc, int nx, int ny, int nz, double *U_aos, double *E_aos, const char *ufile,
+                            const char *efile);
+/* the lattice's state to / from such files (through tcym_lattice_download / _upload) */
+int tcym_lattice_save(tcym_lattice lat, const char *ufile, const char *efile);
+int tcym_lattice_load(tcym_lattice lat, const char *ufile, const char *efile);
 /* U_mu(x) = exp(i t^a theta^a), theta^a = sigma * N(0,1) from the Philox link stream. */
 int tcym_random_links(tcym_lattice lat, double sigma, uint64_t seed);
 /* GaussLawRestoration::Restore (GAUSSLAWFIXING/GaussRestore.cpp:131-167): iterate

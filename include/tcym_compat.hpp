@@ -332,6 +332,7 @@ inline long int MySEED = 0;  // seeds the Philox streams of the compat layer
 
 namespace IO {
 inline std::string OutputDirectory;  // with a trailing '/', as IO/OutputManagement.cpp sets it
+inline std::string InputDirectory, InputUFile, InputEFile;
 }
 
 namespace ThermalDynamics {
@@ -513,6 +514,27 @@ inline DOUBLE GetDeltaNCs(INT NOrder) {
 }
 }  // namespace CoolingMethod
 }  // namespace ChernSimonsNumber
+
+namespace IO {
+// SaveConfiguration (IO/SaveConfiguration.cpp:3-56): <OutputDirectory><Ufname>ID<seed>.txt and the E file
+inline void SaveConfiguration(const std::string &Ufname, const std::string &Efname, GaugeLinks *U,
+                              ElectricFields *E) {
+    const std::string seed = std::to_string(RandomNumberGenerator::MySEED);
+    const std::string uf = OutputDirectory + Ufname + "ID" + seed + ".txt";
+    const std::string ef = OutputDirectory + Efname + "ID" + seed + ".txt";
+    tcym_compat::check(tcym_lattice_save(tcym_compat::bind(U, E), uf.c_str(), ef.c_str()), "save configuration");
+}
+inline void SaveConfiguration(const std::string &Ufname, const std::string &Efname) {
+    SaveConfiguration(Ufname, Efname, GLinks::U, EFields::E);
+}
+// LoadConfiguration (IO/LoadConfiguration.cpp:3-120): <InputDirectory><InputUFile>, <InputDirectory><InputEFile>
+inline void LoadConfiguration(GaugeLinks *U, ElectricFields *E) {
+    const std::string uf = InputDirectory + InputUFile, ef = InputDirectory + InputEFile;
+    // after bind() the device copy is the newest; the host mirrors pull it on their next Get()
+    tcym_compat::check(tcym_lattice_load(tcym_compat::bind(U, E), uf.c_str(), ef.c_str()), "load configuration");
+}
+inline void LoadConfiguration() { LoadConfiguration(GLinks::U, EFields::E); }
+}  // namespace IO
 
 namespace Observables {
 namespace Bulk {

@@ -229,6 +229,7 @@ class Ref:
         L.ref_flow.argtypes = [ctypes.c_double, ctypes.c_int, ctypes.c_int]
         L.ref_flow.restype = ctypes.c_double
         L.ref_thermal_efield.argtypes = [ctypes.c_double, ctypes.c_uint64]
+        L.ref_save_configuration.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_uint64]
         L.ref_cooling_init.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double]
         L.ref_cooling_update.argtypes = [ctypes.c_int]
         L.ref_cooling_update.restype = ctypes.c_double
@@ -283,6 +284,12 @@ class Ref:
         out = np.zeros(16)
         self.lib.ref_observables(_p(out))
         return out
+
+    def save_configuration(self, outdir, ufname, efname, seed):
+        """IO::SaveConfiguration; returns the two file paths."""
+        import os
+        self.lib.ref_save_configuration(str(outdir).encode(), ufname.encode(), efname.encode(), seed)
+        return (os.path.join(str(outdir), f"{ufname}ID{seed}.txt"), os.path.join(str(outdir), f"{efname}ID{seed}.txt"))
 
     def cooling_init(self, blocking, max_steps, block_frequency, sqrt_dctau):
         self.lib.ref_cooling_init(blocking, max_steps, block_frequency, sqrt_dctau)

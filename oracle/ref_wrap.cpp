@@ -101,6 +101,7 @@ DOUBLE Qs = 1.0;
 #include "TOPOLOGY/VacuumEstimator.cpp"
 #include "GRADIENTFLOW/Cooling.cpp"
 #include "TOPOLOGY/CoolingMethod.cpp"
+#include "IO/SaveConfiguration.cpp"
 
 static bool g_langevin_ready = false;
 
@@ -233,6 +234,14 @@ void ref_matrix_ilog(double c, const double *v, double *out) {
     SU_Nc_FUNDAMENTAL_FORMAT m[SUNcGroup::MatrixSize];
     std::memcpy(m, v, sizeof(m));
     SUNcAlgebra::Operations::MatrixILog(c, m, out);
+}
+
+/* IO::SaveConfiguration (IO/SaveConfiguration.cpp:3-56): writes
+ * <outdir>/<ufname>ID<seed>.txt and <outdir>/<efname>ID<seed>.txt. */
+void ref_save_configuration(const char *outdir, const char *ufname, const char *efname, uint64_t seed) {
+    IO::OutputDirectory = StringManipulation::StringCast(outdir, "/");
+    RandomNumberGenerator::MySEED = (long int)seed;
+    IO::SaveConfiguration(ufname, efname);
 }
 
 /* Observables: Bulk (OBSERVABLES/BulkObservables.cpp:133-143), GaussLaw

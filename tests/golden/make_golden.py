@@ -19,6 +19,10 @@ CUDA library draws); every output below is produced by the reference itself:
                            lattice from U = 1, beta 2, seed 7, dTau 0.0375 (20
                            steps a round): final U, E and the ThermalEnergy file
                            (every 20 steps; the reference writes 6 digits)
+  ref_config_su{2,3}_U.txt, ref_config_su{2,3}_E.txt, ref_config_su{2,3}.npz
+                           IO::SaveConfiguration of a random (3,4,5) state (links
+                           seed 21, sigma 0.6; fields seed 22, sigma 0.7): the
+                           reference's text files and the arrays they hold
   ref_cooling_su2.npz      ChernSimonsNumber::CoolingMethod, SU(2) (6,6,6): a
                            random-link state (seed 3, sigma 0.5; E seed 4, 0.7,
                            restored); Start, then 3 x (20 leapfrog steps at dt
@@ -127,6 +131,23 @@ def thermalize(nc):
                         shape=np.array(shape), beta=2.0, seed=7, rounds=2, max_time=0.75, dtau=0.0375)
 
 
+def configuration(nc):
+    import shutil
+    import tempfile
+    P, R = oracle.Port(nc), oracle.Ref(nc)
+    shape = (3, 4, 5)
+    U, E = oracle.empty_fields(nc, shape)
+    P.random_links(shape, U, 0.6, 21)
+    P.gaussian_efield(shape, E, 0.7, 22)
+    R.init(shape)
+    R.set(U, E)
+    with tempfile.TemporaryDirectory() as d:
+        uf, ef = R.save_configuration(d, "Links", "Fields", 9)
+        shutil.copy(uf, os.path.join(HERE, f"ref_config_su{nc}_U.txt"))
+        shutil.copy(ef, os.path.join(HERE, f"ref_config_su{nc}_E.txt"))
+    np.savez_compressed(os.path.join(HERE, f"ref_config_su{nc}.npz"), U=U, E=E, shape=np.array(shape))
+
+
 def cooling():
     P, R = oracle.Port(2), oracle.Ref(2)
     shape = (6, 6, 6)
@@ -158,6 +179,8 @@ if __name__ == "__main__":
     for nc in (2, 3):
         thermalize(nc)
     cooling()
+    for nc in (2, 3):
+        configuration(nc)
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))

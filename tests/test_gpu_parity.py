@@ -276,3 +276,27 @@ def test_cooled_delta_ncs_parity(ctx, oracle_port, nc, prec):
     ref2 = P.cooled_delta_ncs(shape, old, new, 2)
     assert abs(cool.delta_ncs(2) - ref2) <= (1e-9 if prec == tcym.FP64 else 1e-3) * max(abs(ref2), 1e-3)
     cool.close()
+
+
+@pytest.mark.parametrize("prec", PREC)
+@pytest.mark.parametrize("nc", GROUPS)
+def test_configuration_files_round_trip(ctx, oracle_port, tmp_path, nc, prec):
+    """tcym_lattice_save writes what tcym_write_configuration writes for the downloaded
+    state; tcym_lattice_load of those files restores it (FP64: to the 15 digits of the
+    format; FP32: the stored values exactly)."""
+    shape = (4, 3, 6)
+    P = oracle_port[nc]
+    U, E = random_state(P, nc, shape, seed=31)
+    lat = tcym.Lattice(ctx, nc, shape, prec)
+    lat.upload(U, E)
+    Ud, Ed = lat.download()
+    lat.save(tmp_path / "U.txt", tmp_path / "E.txt")
+    tcym.write_configuration(nc, shape, Ud, Ed, tmp_path / "U2.txt", tmp_path / "E2.txt")
+    assert (tmp_path / "U.txt").read_bytes() == (tmp_path / "U2.txt").read_bytes()
+    assert (tmp_path / "E.txt").read_bytes() == (tmp_path / "E2.txt").read_bytes()
+    other = tcym.Lattice(ctx, nc, shape, prec)
+    other.set_zero()
+    other.load(tmp_path / "U.txt", tmp_path / "E.txt")
+    U2, E2 = other.download()
+    tol = 1e-14 if prec == tcym.FP64 else 0.0
+    assert np.abs(U2 - Ud).max() <= tol and np.abs(E2 - Ed).max() <= tol * np.abs(Ed).max()

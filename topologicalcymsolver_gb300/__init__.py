@@ -119,6 +119,12 @@ def library() -> ctypes.CDLL:
         "tcym_lattice_stream": ([ctypes.c_void_p, c_void_pp], ctypes.c_int),
         "tcym_set_zero": ([ctypes.c_void_p], ctypes.c_int),
         "tcym_gaussian_efield": ([ctypes.c_void_p, ctypes.c_double, ctypes.c_uint64], ctypes.c_int),
+        "tcym_write_configuration": ([ctypes.c_int] * 4 + [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_char_p,
+                                                          ctypes.c_char_p], ctypes.c_int),
+        "tcym_read_configuration": ([ctypes.c_int] * 4 + [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_char_p,
+                                                         ctypes.c_char_p], ctypes.c_int),
+        "tcym_lattice_save": ([ctypes.c_void_p, ctypes.c_char_p, ctypes.c_char_p], ctypes.c_int),
+        "tcym_lattice_load": ([ctypes.c_void_p, ctypes.c_char_p, ctypes.c_char_p], ctypes.c_int),
         "tcym_cooling_create": ([ctypes.c_void_p, ctypes.c_int, ctypes.c_double, c_void_pp], ctypes.c_int),
         "tcym_cooling_destroy": ([ctypes.c_void_p], ctypes.c_int),
         "tcym_cooling_start": ([ctypes.c_void_p], ctypes.c_int),
@@ -284,6 +290,14 @@ class Lattice:
                                                 series.ctypes.data_as(ctypes.c_void_p), cap, ctypes.byref(n)))
         return series[:n.value].copy()
 
+    def save(self, ufile=None, efile=None):
+        """The state to the reference's configuration text files (IO::SaveConfiguration)."""
+        self.ctx.check(self.lib.tcym_lattice_save(self.h, _path(ufile), _path(efile)))
+
+    def load(self, ufile=None, efile=None):
+        """The state from the reference's configuration text files (IO::LoadConfiguration)."""
+        self.ctx.check(self.lib.tcym_lattice_load(self.h, _path(ufile), _path(efile)))
+
     def random_links(self, sigma: float, seed: int):
         self.ctx.check(self.lib.tcym_random_links(self.h, sigma, seed))
 
@@ -346,6 +360,30 @@ class Lattice:
 
     def ncs_reset(self):
         self.ctx.check(self.lib.tcym_ncs_reset(self.h))
+
+
+def _path(p):
+    return None if p is None else os.fsencode(p)
+
+
+def write_configuration(nc: int, shape, U=None, E=None, ufile=None, efile=None) -> None:
+    """Host arrays (the reference AoS layouts) to the reference's text files; no GPU needed."""
+    rc = library().tcym_write_configuration(nc, *shape, _ptr(U) if U is not None else None,
+                                            _ptr(E) if E is not None else None, _path(ufile), _path(efile))
+    if rc:
+        raise TcymError(rc, "tcym_write_configuration failed")
+
+
+def read_configuration(nc: int, shape, ufile=None, efile=None):
+    """The reference's text files to host arrays (U, E); no GPU needed."""
+    V = int(np.prod(shape))
+    U = np.zeros((V, 3, 4 if nc == 2 else 18)) if ufile else None
+    E = np.zeros((V, 3, 3 if nc == 2 else 8)) if efile else None
+    rc = library().tcym_read_configuration(nc, *shape, _ptr(U) if U is not None else None,
+                                           _ptr(E) if E is not None else None, _path(ufile), _path(efile))
+    if rc:
+        raise TcymError(rc, "tcym_read_configuration: unreadable or incomplete files")
+    return U, E
 
 
 class Cooling:
