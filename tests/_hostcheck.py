@@ -62,7 +62,7 @@ class HostLattice:
         self.U = [np.zeros(3 * LINK_BYTES[self.fmt] * stored, np.uint8) for _ in range(2)]
         self.E = np.zeros(3 * FIELD_BYTES[self.fmt] * stored, np.uint8)
         self.cur = 0
-        self.pairs = 1  # 0: force the per-site step
+        self.pairs = 1  # 0: the per-site step; 1 + tx: the paired step with block tiling tx (0: linear)
 
     def upload(self, U=None, E=None):
         self.L.hc_from_aos(self.fmt, self.n, None if U is None else _p(U), None if E is None else _p(E),

@@ -221,3 +221,24 @@ def test_site_geodesic(oracle_port, nc, prec):
         Uh, Eh = M.download()
         assert rel(Uh, Um) < TOL[prec] and rel(Eh, Em) < TOL[prec]
     assert rel(M.download()[0], Un) < TOL[prec]  # c = 1 lands on UNew
+
+
+@pytest.mark.parametrize("nc", [2, 3])
+def test_pair_step_tilings(oracle_port, nc):
+    """Every block tiling of the paired step (linear, and tx x 128/tx tiles of one z-plane,
+    including tiles wider than the lattice) visits each pair once with the right seam
+    handling: the results are bit-identical across tilings and match the oracle."""
+    P = oracle_port[nc]
+    shape = (12, 10, 8)
+    U, E = _state(P, nc, shape, 41)
+    out = []
+    for tx in (0, 128, 32, 16, 8):
+        H = hc.HostLattice(nc, "f32", shape)
+        H.pairs = 1 + tx
+        H.upload(U, E)
+        H.leapfrog(0.05, 3)
+        out.append(H.download())
+    for Uh, Eh in out[1:]:
+        assert np.array_equal(Uh, out[0][0]) and np.array_equal(Eh, out[0][1])
+    P.leapfrog(shape, U, E, 0.05, 3)
+    assert rel(out[0][0], U) < 1e-5 and rel(out[0][1], E) < 1e-5

@@ -125,6 +125,9 @@ def library() -> ctypes.CDLL:
                                                          ctypes.c_char_p], ctypes.c_int),
         "tcym_lattice_save": ([ctypes.c_void_p, ctypes.c_char_p, ctypes.c_char_p], ctypes.c_int),
         "tcym_lattice_load": ([ctypes.c_void_p, ctypes.c_char_p, ctypes.c_char_p], ctypes.c_int),
+        "tcym_lattice_tile": ([ctypes.c_void_p, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)],
+                              ctypes.c_int),
+        "tcym_lattice_set_tile": ([ctypes.c_void_p, ctypes.c_int, ctypes.c_int], ctypes.c_int),
         "tcym_cooling_create": ([ctypes.c_void_p, ctypes.c_int, ctypes.c_double, c_void_pp], ctypes.c_int),
         "tcym_cooling_destroy": ([ctypes.c_void_p], ctypes.c_int),
         "tcym_cooling_start": ([ctypes.c_void_p], ctypes.c_int),
@@ -289,6 +292,15 @@ class Lattice:
         self.ctx.check(self.lib.tcym_thermalize(self.h, beta, seed, rounds, max_time, dt, restore_tol, every,
                                                 series.ctypes.data_as(ctypes.c_void_p), cap, ctypes.byref(n)))
         return series[:n.value].copy()
+
+    def tile(self):
+        """(tx, ty) of the packed FP32 step's block tiling (autotuned on first use; tx 0: linear)."""
+        tx, ty = ctypes.c_int(), ctypes.c_int()
+        self.ctx.check(self.lib.tcym_lattice_tile(self.h, ctypes.byref(tx), ctypes.byref(ty)))
+        return tx.value, ty.value
+
+    def set_tile(self, tx: int, ty: int = 0):
+        self.ctx.check(self.lib.tcym_lattice_set_tile(self.h, tx, ty))
 
     def save(self, ufile=None, efile=None):
         """The state to the reference's configuration text files (IO::SaveConfiguration)."""

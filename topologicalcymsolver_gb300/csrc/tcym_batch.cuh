@@ -23,6 +23,7 @@ template <class T> struct Member {
     int red_begin;       // first reduction work item of this member
     int red_blocks;      // reduction work items of this member
     int paired;          // step work items cover site pairs (FP32 format, even nz)
+    Tile tile;           // their block tiling
     double ncs_dt;       // Kahan increment factor for measurements (0: no N_CS update)
 };
 
@@ -56,13 +57,12 @@ __global__ void __launch_bounds__(threads_for<FMT>(), batch_min_blocks_for<FMT>(
         const Geom g = m.g;
         if constexpr (Fmt<FMT>::PAIRED) {
             if (m.paired) {  // block-uniform
-                const int64_t p0 = (int64_t)(item - m.block_begin) * blockDim.x, p = p0 + threadIdx.x;
-                if (p < (g.V >> 1)) {
+                int64_t p;
+                bool seam;
+                if (tile_pair(g, m.tile, item - m.block_begin, threadIdx.x, p, seam)) {
                     const int in = m.cur ^ (k & 1);
-                    if (pairs_touch_seam(g, p0, blockDim.x))
-                        site_step_pair<Fmt<FMT>, true>(g, m.U[in], m.U[in ^ 1], m.E, m.c, p, (uint64_t)k);
-                    else
-                        site_step_pair<Fmt<FMT>, false>(g, m.U[in], m.U[in ^ 1], m.E, m.c, p, (uint64_t)k);
+                    if (seam) site_step_pair<Fmt<FMT>, true>(g, m.U[in], m.U[in ^ 1], m.E, m.c, p, (uint64_t)k);
+                    else site_step_pair<Fmt<FMT>, false>(g, m.U[in], m.U[in ^ 1], m.E, m.c, p, (uint64_t)k);
                 }
                 continue;
             }

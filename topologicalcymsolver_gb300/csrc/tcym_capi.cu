@@ -470,8 +470,9 @@ int tcym_run_steps(tcym_lattice lat, int mode, double dt, double gamma, double T
     cudaSetDevice(ctx->device);
     for (int i = 0; i < nsteps; ++i) {
         StepCoef<double> c = tcym_coef(lat->a, mode, dt, gamma, T, seed, step0 + (uint64_t)i);
+        const Tile &t = tcym_lattice_tile_of(lat);
         DISPATCH(lat->fmt,
-                 CK(L::step(lat->g, lat->U[lat->cur], lat->U[1 - lat->cur], lat->E, c, true, true, lat->stream)));
+                 CK(L::step(lat->g, lat->U[lat->cur], lat->U[1 - lat->cur], lat->E, c, true, true, lat->stream, t)));
         lat->cur ^= 1;
         ++lat->steps_done;
         int r = maybe_reunitarize(lat);
@@ -529,8 +530,9 @@ extern "C" int tcym_flow(tcym_lattice lat, double dtau, int nsteps, int mode, in
     for (int s = 0; s < nsteps; ++s) {
         if (mode == TCYM_FLOW_SIMULTANEOUS) {
             // F into E and U' = exp(-i dtau F) U into the other buffer; U stays intact
+            const Tile &t = tcym_lattice_tile_of(lat);
             DISPATCH(lat->fmt, CK(L::step(lat->g, lat->U[lat->cur], lat->U[1 - lat->cur], lat->E, c, true, true,
-                                          lat->stream)));
+                                          lat->stream, t)));
         } else {
             if (calibrate)  // the force of the state before the sweep, for the trapezoid rule
                 DISPATCH(lat->fmt, CK(L::step(lat->g, lat->U[lat->cur], lat->U[lat->cur], lat->E, c, true, false,

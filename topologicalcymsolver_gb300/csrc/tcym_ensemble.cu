@@ -94,7 +94,8 @@ template <int FMT> static void fill_group(tcym_ensemble ens, FmtGroup &G, int sm
         m.cur = L->cur;
         m.block_begin = blk;
         m.paired = Fmt<FMT>::PAIRED && L->g.nz % 2 == 0;
-        blk += grid_for(m.paired ? L->g.V / 2 : L->g.V, TPB);
+        m.tile = m.paired ? tcym_lattice_tile_of(L) : Tile{0, 0, 0, 0, 0};
+        blk += m.paired ? (int)tile_blocks(L->g, m.tile) : grid_for(L->g.V, TPB);
         m.red_begin = red;
         m.red_blocks = grid_for(L->g.V, kRedThreads);
         red += m.red_blocks;

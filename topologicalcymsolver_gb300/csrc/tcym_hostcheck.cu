@@ -47,20 +47,22 @@ template <class T> StepCoef<T> cast(const StepCoef<double> &c) {
 template <int FMT> struct H {
     using F = Fmt<FMT>;
     using T = typename F::T;
+    // pairs: 0 per-site step; 1 + tx: the paired step with tiling tx (0: linear)
     static void step(const Geom &g, const void *Uin, void *Uout, void *E, const StepCoef<double> &cd, int doE,
                      int doU, int pairs) {
         StepCoef<T> c = cast<T>(cd);
         if constexpr (F::PAIRED) {
-            // the device's paired step, block by block as the kernel runs it (128 pairs a block)
+            // the device's paired step, block by block and thread by thread as the kernel runs it
             if (pairs && doE && doU && g.nz % 2 == 0) {
-                const int64_t Vh = g.V / 2;
-                for (int64_t p0 = 0; p0 < Vh; p0 += 128) {
-                    const bool seam = pairs_touch_seam(g, p0, 128);
-                    for (int64_t p = p0; p < p0 + 128 && p < Vh; ++p) {
+                const Tile t = make_tile(g, pairs - 1);
+                for (int64_t b = 0; b < tile_blocks(g, t); ++b)
+                    for (int tid = 0; tid < 128; ++tid) {
+                        int64_t p;
+                        bool seam;
+                        if (!tile_pair(g, t, b, tid, p, seam)) continue;
                         if (seam) site_step_pair<F, true>(g, Uin, Uout, E, c, p);
                         else site_step_pair<F, false>(g, Uin, Uout, E, c, p);
                     }
-                }
                 return;
             }
         }
@@ -182,7 +184,8 @@ int hc_to_aos(int fmt, const int *n, const void *U, const void *E, double *Ua, d
     HC_DISPATCH(fmt, for (int64_t s = 0; s < g.V; ++s) site_to_aos<HH::F>(g, U, E, Ua, Ea, s));
     return 0;
 }
-// pairs: take the paired step where the device does (FP32 formats, even nz, fused step)
+// pairs: 0 the per-site step; 1 + tx: the paired step where the device takes it (FP32
+// formats, even nz, fused step) with block tiling tx (0: linear)
 int hc_step(int fmt, const int *n, const void *Uin, void *Uout, void *E, int mode, double dt, double gamma, double T,
             uint64_t seed, uint64_t step, int doE, int doU, int pairs) {
     Geom g = geom(n);

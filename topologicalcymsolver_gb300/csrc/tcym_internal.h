@@ -3,6 +3,8 @@
 
 #include <cuda_runtime.h>
 
+#include <array>
+#include <map>
 #include <mutex>
 #include <string>
 
@@ -14,6 +16,8 @@ struct tcym_ctx_s {
     int sm_count = 152;
     std::mutex mu;
     std::string last_error;
+    std::mutex tune_mu;
+    std::map<std::array<int, 4>, tcym::Tile> tiles;  // autotuned paired-step tiling per (format, nx, ny, nz)
 };
 
 struct tcym_lattice_s {
@@ -36,6 +40,8 @@ struct tcym_lattice_s {
     int reunit_period = 0, steps_since_reunit = 0;
     int ncs_every = 0;
     int64_t steps_done = 0;
+    tcym::Tile tile{};   // block tiling of the paired step
+    bool tile_chosen = false;
 };
 
 void tcym_set_error(tcym_ctx ctx, const char *fmt, ...);
@@ -48,5 +54,7 @@ tcym::StepCoef<double> tcym_coef(const double *a, int mode, double dt, double ga
 int tcym_reduce(tcym_lattice lat, int mask, double ncs_dt);
 // frees the Gauss-restore and AoS staging scratch of a lattice (reallocated on next use)
 void tcym_lattice_release_scratch(tcym_lattice lat);
+// the block tiling of lat's paired step, autotuned on first use (tcym_autotune.cu)
+const tcym::Tile &tcym_lattice_tile_of(tcym_lattice lat);
 int tcym_run_steps(tcym_lattice lat, int mode, double dt, double gamma, double T, uint64_t seed, uint64_t step0,
                    int nsteps);

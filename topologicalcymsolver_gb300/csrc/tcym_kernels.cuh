@@ -90,11 +90,12 @@ __global__ void __launch_bounds__(threads_for<FMT>(), min_blocks_for<FMT>()) k_s
 // take the lane-swapping loads
 template <int FMT>
 __global__ void __launch_bounds__(kThreadsPair, pair_min_blocks_for<FMT>())
-    k_step_pair(Geom g, const void *Uin, void *Uout, void *E, StepCoef<float> c) {
-    const int64_t p0 = (int64_t)blockIdx.x * blockDim.x, p = p0 + threadIdx.x;
-    if (p >= (g.V >> 1)) return;
+    k_step_pair(Geom g, const void *Uin, void *Uout, void *E, StepCoef<float> c, Tile t) {
+    int64_t p;
+    bool seam;
+    if (!tile_pair(g, t, blockIdx.x, threadIdx.x, p, seam)) return;
 #if TCYM_PAIR_SEAM_SPLIT
-    if (pairs_touch_seam(g, p0, blockDim.x)) site_step_pair<Fmt<FMT>, true>(g, Uin, Uout, E, c, p);
+    if (seam) site_step_pair<Fmt<FMT>, true>(g, Uin, Uout, E, c, p);
     else site_step_pair<Fmt<FMT>, false>(g, Uin, Uout, E, c, p);
 #else
     site_step_pair<Fmt<FMT>, true>(g, Uin, Uout, E, c, p);
@@ -240,12 +241,13 @@ template <int FMT> struct Launch {
     using T = typename F::T;
     static constexpr int TPB = threads_for<FMT>();
 
+    // t: the block tiling of the paired step (FP32 formats with even nz)
     static cudaError_t step(const Geom &g, const void *Uin, void *Uout, void *E, const StepCoef<double> &cd, bool doE,
-                            bool doU, cudaStream_t st) {
+                            bool doU, cudaStream_t st, const Tile &t = Tile{0, 0, 0, 0, 0}) {
         StepCoef<T> c = coef_cast<T>(cd);
         if constexpr (F::PAIRED) {
             if (doE && doU && g.nz % 2 == 0) {
-                k_step_pair<FMT><<<grid_for(g.V >> 1, kThreadsPair), kThreadsPair, 0, st>>>(g, Uin, Uout, E, c);
+                k_step_pair<FMT><<<(unsigned)tile_blocks(g, t), kThreadsPair, 0, st>>>(g, Uin, Uout, E, c, t);
                 return cudaGetLastError();
             }
         }

@@ -179,6 +179,45 @@ TCYM_HD bool pairs_touch_seam(const Geom &g, int64_t p0, int64_t n) {
     return p0 < plane || last >= Vh - plane;
 }
 
+// How the paired step's blocks of 128 threads cover the pairs: tx = 0, 128
+// consecutive pair indices (rows run on); otherwise a tx x ty tile (tx = 2^lx,
+// tx * ty = 128) of one z-plane, so the +-y neighbours of most pairs are in the
+// block's own L1 working set.  Chosen per lattice shape by the autotuner.
+struct Tile {
+    int tx, ty, lx;          // tile extents; lx = log2(tx)
+    int tiles_x, tiles_y;    // tiles per z-plane
+};
+// tx = 0: linear; else a tx x (128 / tx) tile, tx a power of two from 1 to 128
+TCYM_HD Tile make_tile(const Geom &g, int tx) {
+    if (tx <= 0) return Tile{0, 0, 0, 0, 0};
+    int lx = 0;
+    while ((1 << lx) < tx) ++lx;
+    const int ty = 128 / tx;
+    return Tile{tx, ty, lx, (g.nx + tx - 1) / tx, (g.ny + ty - 1) / ty};
+}
+TCYM_HD int64_t tile_blocks(const Geom &g, const Tile &t) {
+    const int64_t Vh = g.V >> 1;
+    if (t.tx == 0) return (Vh + 127) / 128;
+    return (int64_t)t.tiles_x * t.tiles_y * (g.nz >> 1);
+}
+// Pair of thread `tid` in block `b`, and whether the block touches the seam;
+// false: the thread has no pair (a partial tile or the last linear block).
+TCYM_HD bool tile_pair(const Geom &g, const Tile &t, int64_t b, int tid, int64_t &p, bool &seam) {
+    if (t.tx == 0) {
+        p = b * 128 + tid;
+        seam = pairs_touch_seam(g, b * 128, 128);
+        return p < (g.V >> 1);
+    }
+    const int64_t per_plane = (int64_t)t.tiles_x * t.tiles_y;
+    const int z = (int)(b / per_plane);
+    const int r = (int)(b - (int64_t)z * per_plane);
+    const int by = r / t.tiles_x, bx = r - by * t.tiles_x;
+    const int x = bx * t.tx + (tid & (t.tx - 1)), y = by * t.ty + (tid >> t.lx);
+    seam = z == 0 || z == (g.nz >> 1) - 1;
+    p = x + (int64_t)g.nx * (y + (int64_t)g.ny * z);
+    return x < g.nx && y < g.ny;
+}
+
 // Checkerboard flow: one link U_mu(x) of the active parity moved in place by
 // exp(-i dtau F_mu(x)), F = fc proj(U_mu A) (no reference counterpart; the
 // reference flows all links at once, GradientFlow.cpp:150-165).
