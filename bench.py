@@ -270,6 +270,7 @@ def run_ours(a):
                    "tcym_leapfrog step, tcym_lattice_download of the new state"}
 
     med = statistics.median(per)
+    tile = "x".join(map(str, lat.tile())) if L % 2 == 0 else "per-site step (odd extent)"
     peak, peak_kind = measured_peak()
     achieved = BYTES_PER_LINK * links / med / 1e9
     traffic = ncu_traffic()
@@ -284,7 +285,7 @@ def run_ours(a):
     if rank == 0:
         out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": a.steps, "warmup": a.warmup,
                "ms_per_step": total / a.steps * 1e3, "higher_is_better": True, "scaling": "weak",
-               "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config(L, dt),
+               "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": dict(config(L, dt), tile=tile),
                "e2e": e2e, "roofline": roof, "clocks": clk.summary(), "gpu_launches": a.steps + reunits,
                "impl": "ours"}
         if ws == 1 and not a.no_cpu_baseline:

@@ -140,8 +140,8 @@ int tcym_thermalize(tcym_lattice lat, double beta, uint64_t seed, int rounds, do
 /* Block tiling of the packed FP32 step (FP32 lattices with even nz; no reference
  * counterpart): each block of 128 threads advances tx x ty site pairs of one z-plane,
  * or, for tx = 0, 128 consecutive pairs.  Chosen on the lattice's first step by an
- * autotuner that times the candidates on a proxy lattice with the same nx, ny (and
- * at most 16 planes), cached per format and extents in the context; TCYM_TILE=linear
+ * autotuner that times the candidates on a proxy lattice with the same nx, ny (at most
+ * 1 GiB), cached per format and extents in the context; TCYM_TILE=linear
  * or TCYM_TILE=<tx>x<ty> in the environment overrides it.  Results do not depend on
  * the tiling.  tcym_lattice_set_tile fixes it (tx a power of two, tx * ty = 128, or
  * tx = 0) or, with tx = -1, hands it back to the autotuner. */

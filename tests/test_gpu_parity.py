@@ -300,3 +300,28 @@ def test_configuration_files_round_trip(ctx, oracle_port, tmp_path, nc, prec):
     U2, E2 = other.download()
     tol = 1e-14 if prec == tcym.FP64 else 0.0
     assert np.abs(U2 - Ud).max() <= tol and np.abs(E2 - Ed).max() <= tol * np.abs(Ed).max()
+
+
+@pytest.mark.parametrize("nc", GROUPS)
+def test_step_tilings_identical(ctx, oracle_port, nc):
+    """The packed FP32 step's block tilings (linear and tx x ty tiles, one wider than the
+    lattice) give bit-identical results; the autotuner picks one of the candidates."""
+    shape = (24, 20, 16)
+    P = oracle_port[nc]
+    U, E = random_state(P, nc, shape, seed=51)
+    results = []
+    for tx in (0, 32, 16, 8, 128):
+        lat = tcym.Lattice(ctx, nc, shape, tcym.FP32)
+        lat.set_tile(tx, 0 if tx == 0 else 128 // tx)
+        lat.upload(U, E)
+        lat.leapfrog(0.05, 4)
+        lat.langevin(0.02, 1.0, 0.6, 3, 0, 2)
+        results.append(lat.download())
+        lat.close()
+    for Ug, Eg in results[1:]:
+        assert np.array_equal(Ug, results[0][0]) and np.array_equal(Eg, results[0][1])
+    auto = tcym.Lattice(ctx, nc, shape, tcym.FP32)
+    tx, ty = auto.tile()
+    assert tx == 0 or (tx * ty == 128 and tx <= shape[0] and ty <= shape[1])
+    with pytest.raises(tcym.TcymError):
+        auto.set_tile(48, 2)

@@ -5,13 +5,15 @@
 // of a pair's +-x and +-y neighbour links the block itself has just loaded,
 // i.e. the L1 reuse, and what share of the threads idle on ragged planes.  The
 // best choice depends on nx and ny, so the first step of a lattice times the
-// candidates on a proxy lattice of the same format, nx and ny and at most 16
-// planes in z (a few launches each, CUDA events on the proxy's stream), and the
-// context keeps the winner per (format, nx, ny, nz).  A site's arithmetic does
+// candidates on a proxy lattice of the same format, nx and ny (at most 1 GiB;
+// best of three trials of ~2 ms each, CUDA events on the proxy's stream), and
+// the context keeps the winner per (format, nx, ny, nz); a tile must beat the
+// linear mapping by 3% to be taken.  A site's arithmetic does
 // not depend on the tiling, only the speed does.
 //
 // TCYM_TILE=linear or TCYM_TILE=<tx>x<ty> in the environment, or
 // tcym_lattice_set_tile, fixes the tiling instead.
+#include <algorithm>
 #include <cstdlib>
 #include <cstring>
 #include <vector>
@@ -77,31 +79,40 @@ float time_tile(tcym_lattice p, const Tile &t, int reps) {
     return ms;
 }
 
-// the fastest candidate on a proxy lattice; linear when anything fails
+// The fastest candidate on a proxy lattice; linear unless a tile beats it by 3%
+// (timing noise must not pick a slower tiling), and linear when anything fails.
+// The proxy has the lattice's nx and ny and as many z-planes as keep it under
+// 1 GiB, so that a lattice larger than L2 is timed out of HBM as it runs.
 Tile tune(tcym_lattice lat) {
-    Tile best = make_tile(lat->g, 0);
+    const Tile linear = make_tile(lat->g, 0);
     const std::vector<Tile> cand = candidates(lat->g);
-    if (cand.size() < 2) return best;
-    const int nzp = lat->g.nz < 16 ? lat->g.nz : 16;
+    if (cand.size() < 2) return linear;
+    const size_t per_plane = 3 * (2 * tcym_link_bytes(lat->fmt) + tcym_field_bytes(lat->fmt)) *
+                             (size_t)lat->g.nx * (size_t)lat->g.ny;
+    int nzp = (int)std::min<size_t>((size_t)lat->g.nz, ((size_t)1 << 30) / per_plane);
+    nzp = std::max(2, nzp & ~1);
     tcym_lattice p = nullptr;
-    if (tcym_lattice_create_ex(lat->ctx, lat->nc, lat->g.nx, lat->g.ny, nzp, lat->a, lat->precision, &p)) return best;
+    if (tcym_lattice_create_ex(lat->ctx, lat->nc, lat->g.nx, lat->g.ny, nzp, lat->a, lat->precision, &p))
+        return linear;
     if (tcym_random_links(p, 0.5, 1) || tcym_gaussian_efield(p, 0.7, 2)) {
         tcym_lattice_destroy(p);
-        return best;
+        return linear;
     }
-    const int reps = p->g.V > (1 << 16) ? 5 : 20;
-    float best_ms = -1.f;
-    for (const Tile &t : cand) {
-        // tile geometry for the proxy's extents (same nx, ny: same tiles per plane)
-        const float ms = time_tile(p, t, reps);
-        if (ms > 0.f && (best_ms < 0.f || ms < best_ms)) {
-            best_ms = ms;
-            best = make_tile(lat->g, t.tx);
+    // launches per trial: about 2 ms of work at ~1e10 link-updates/s
+    const int reps = (int)std::max<int64_t>(5, std::min<int64_t>(200, 20000000 / (3 * p->g.V)));
+    std::vector<float> ms(cand.size(), -1.f);
+    for (int trial = 0; trial < 3; ++trial)  // best of three, candidates interleaved
+        for (size_t i = 0; i < cand.size(); ++i) {
+            const float t = time_tile(p, cand[i], reps);
+            if (t > 0.f && (ms[i] < 0.f || t < ms[i])) ms[i] = t;
         }
-    }
     cudaGetLastError();  // a failed candidate leaves nothing behind but its error
     tcym_lattice_destroy(p);
-    return best;
+    size_t best = 0;
+    for (size_t i = 1; i < cand.size(); ++i)
+        if (ms[i] > 0.f && (ms[best] < 0.f || ms[i] < ms[best])) best = i;
+    if (best != 0 && ms[0] > 0.f && ms[best] > 0.97f * ms[0]) best = 0;
+    return make_tile(lat->g, cand[best].tx);
 }
 
 }  // namespace

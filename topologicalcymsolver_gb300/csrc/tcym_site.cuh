@@ -106,7 +106,10 @@ TCYM_HD void site_step(const Geom &g, const void *Uin, void *Uout, void *E, cons
 #ifndef TCYM_PAIR_STAPLE_UNROLL
 #define TCYM_PAIR_STAPLE_UNROLL 2
 #endif
-constexpr int kPairStapleUnroll = TCYM_PAIR_STAPLE_UNROLL;  // 1: one copy of the staple code for both planes
+constexpr int kPairStapleUnroll = TCYM_PAIR_STAPLE_UNROLL;
+#ifndef TCYM_PAIR_LATE_LOADS
+#define TCYM_PAIR_LATE_LOADS 0
+#endif  // 1: one copy of the staple code for both planes
 // site_step for both sites of pair p of an FP32 lattice with even nz, (x,y,z)
 // and (x,y,z+nz/2), in packed FP32 (f2): the same staples, projection, E
 // update and exponential per lane, at half the instructions.  SEAM: the pair
@@ -146,10 +149,19 @@ TCYM_HD void site_step_pair(const Geom &g, const void *Uin, void *Uout, void *E,
     const PairNbhd nb(g, p);
 #pragma unroll 1
     for (int mu = 0; mu < 3; ++mu) {
+#if TCYM_PAIR_LATE_LOADS
+        // the link and its field are read after the staple sum, so that they are
+        // not live (36 + 16 registers) while it runs
+        const M2 A = staple_sum_pair<F, SEAM>(Uin, Vh, nb, mu, c.cnu);
+        const M2 u = F::load2(Uin, Vh, mu, p, false);
+        f2 e[NA];
+        F::load_e2(E, Vh, mu, p, e);
+#else
         f2 e[NA];
         F::load_e2(E, Vh, mu, p, e);
         const M2 u = F::load2(Uin, Vh, mu, p, false);
         const M2 A = staple_sum_pair<F, SEAM>(Uin, Vh, nb, mu, c.cnu);
+#endif
         f2 f[NA];
         G2::proj_mul(u, A, f);
         const f2 fc(sel3(c.fc, mu));
