@@ -79,11 +79,12 @@ def test_observable_errors(ctx, oracle_port, config, prec):
     print(f"\n{config} {'FP64' if prec == tcym.FP64 else 'FP32'} max relative error over 100 steps:")
     for name, e in zip(NAMES, err):
         print(f"  {name:14s} {e:.2e}")
-    # violations are tiny absolute numbers (~1e-14 in FP64, ~1e-7 in FP32): bound them absolutely
     for i, name in enumerate(NAMES):
-        if name in ("Gauss |max|", "Gauss rms", "unitarity max"):
+        if name == "unitarity max" or (config == "c0" and name.startswith("Gauss")):
+            # violations of a restored / unitary state are rounding-level absolute numbers
+            # (~1e-14 in FP64, ~1e-7 in FP32): bounded absolutely
             assert np.abs(got[:, i]).max() < (1e-10 if prec == tcym.FP64 else 1e-4), name
-        else:
+        else:  # the Langevin noise breaks Gauss's law (config 1): its violation compares relatively
             assert err[i] < tol, (name, err[i])
 
 

@@ -147,6 +147,10 @@ static void lattice_free(tcym_lattice lat) {
     cudaFree(lat->gauss);
     cudaFree(lat->staging);
     if (lat->host_result) cudaFreeHost(lat->host_result);
+    for (int i = 0; i < 2; ++i)
+        if (lat->side[i]) cudaStreamDestroy(lat->side[i]);
+    for (int i = 0; i < 3; ++i)
+        if (lat->ev[i]) cudaEventDestroy(lat->ev[i]);
     if (lat->stream) cudaStreamDestroy(lat->stream);
 }
 
@@ -220,6 +224,10 @@ static int ensure_staging(tcym_lattice lat) {
     tcym_ctx ctx = lat->ctx;
     const int nmd = lat->nc == 2 ? 4 : 18, na = lat->nc == 2 ? 3 : 8;
     const size_t need = sizeof(double) * 3 * (size_t)(nmd + na) * (size_t)lat->g.V;
+    for (int i = 0; i < 2; ++i)
+        if (!lat->side[i]) CK(cudaStreamCreateWithFlags(&lat->side[i], cudaStreamNonBlocking));
+    for (int i = 0; i < 3; ++i)
+        if (!lat->ev[i]) CK(cudaEventCreateWithFlags(&lat->ev[i], cudaEventDisableTiming));
     if (lat->staging_bytes >= need) return TCYM_OK;
     cudaFree(lat->staging);
     lat->staging = nullptr;
@@ -229,6 +237,26 @@ static int ensure_staging(tcym_lattice lat) {
     return TCYM_OK;
 }
 
+// host transfers in chunks of about 64 MB (at most 32), at least one
+static int64_t transfer_chunks(tcym_lattice lat, bool u, bool e) {
+    const int nmd = lat->nc == 2 ? 4 : 18, na = lat->nc == 2 ? 3 : 8;
+    const int64_t bytes = (int64_t)sizeof(double) * 3 * ((u ? nmd : 0) + (e ? na : 0)) * lat->g.V;
+    int64_t k = bytes / (64ll << 20);
+    if (k < 1) k = 1;
+    if (k > 32) k = 32;
+    if (k > lat->g.V) k = lat->g.V;
+    return k;
+}
+// the lattice's stream waits for both side streams
+static cudaError_t join_side(tcym_lattice lat) {
+    for (int i = 0; i < 2; ++i) {
+        cudaError_t e = cudaEventRecord(lat->ev[1 + i], lat->side[i]);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(lat->stream, lat->ev[1 + i], 0);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
 extern "C" int tcym_lattice_upload(tcym_lattice lat, const double *U_aos, const double *E_aos) {
     if (!lat) return TCYM_ERR_ARG;
     tcym_ctx ctx = lat->ctx;
@@ -236,12 +264,26 @@ extern "C" int tcym_lattice_upload(tcym_lattice lat, const double *U_aos, const 
     int r = ensure_staging(lat);
     if (r) return r;
     const int nmd = lat->nc == 2 ? 4 : 18, na = lat->nc == 2 ? 3 : 8;
-    const size_t V = (size_t)lat->g.V;
+    const int64_t V = lat->g.V;
     double *du = lat->staging, *de = lat->staging + 3 * nmd * V;
-    if (U_aos) CK(cudaMemcpyAsync(du, U_aos, sizeof(double) * 3 * nmd * V, cudaMemcpyHostToDevice, lat->stream));
-    if (E_aos) CK(cudaMemcpyAsync(de, E_aos, sizeof(double) * 3 * na * V, cudaMemcpyHostToDevice, lat->stream));
-    DISPATCH(lat->fmt, CK(L::from_aos(lat->g, lat->U[lat->cur], lat->E, U_aos ? du : nullptr, E_aos ? de : nullptr,
-                                      lat->stream)));
+    // chunks of sites alternate between two side streams, so that the copy of one
+    // chunk overlaps the layout conversion of the previous one (and two copy engines run)
+    const int64_t nchunk = transfer_chunks(lat, U_aos != nullptr, E_aos != nullptr);
+    CK(cudaEventRecord(lat->ev[0], lat->stream));
+    for (int i = 0; i < 2; ++i) CK(cudaStreamWaitEvent(lat->side[i], lat->ev[0], 0));
+    for (int64_t k = 0; k < nchunk; ++k) {
+        const int64_t s0 = V * k / nchunk, s1 = V * (k + 1) / nchunk;
+        cudaStream_t st = lat->side[k & 1];
+        if (U_aos)
+            CK(cudaMemcpyAsync(du + 3 * nmd * s0, U_aos + 3 * nmd * s0, sizeof(double) * 3 * nmd * (s1 - s0),
+                               cudaMemcpyHostToDevice, st));
+        if (E_aos)
+            CK(cudaMemcpyAsync(de + 3 * na * s0, E_aos + 3 * na * s0, sizeof(double) * 3 * na * (s1 - s0),
+                               cudaMemcpyHostToDevice, st));
+        DISPATCH(lat->fmt, CK(L::from_aos(lat->g, lat->U[lat->cur], lat->E, U_aos ? du : nullptr,
+                                          E_aos ? de : nullptr, st, s0, s1 - s0)));
+    }
+    CK(join_side(lat));
     CK(cudaStreamSynchronize(lat->stream));
     return TCYM_OK;
 }
@@ -253,12 +295,24 @@ extern "C" int tcym_lattice_download(tcym_lattice lat, double *U_aos, double *E_
     int r = ensure_staging(lat);
     if (r) return r;
     const int nmd = lat->nc == 2 ? 4 : 18, na = lat->nc == 2 ? 3 : 8;
-    const size_t V = (size_t)lat->g.V;
+    const int64_t V = lat->g.V;
     double *du = lat->staging, *de = lat->staging + 3 * nmd * V;
-    DISPATCH(lat->fmt, CK(L::to_aos(lat->g, lat->U[lat->cur], lat->E, U_aos ? du : nullptr, E_aos ? de : nullptr,
-                                    lat->stream)));
-    if (U_aos) CK(cudaMemcpyAsync(U_aos, du, sizeof(double) * 3 * nmd * V, cudaMemcpyDeviceToHost, lat->stream));
-    if (E_aos) CK(cudaMemcpyAsync(E_aos, de, sizeof(double) * 3 * na * V, cudaMemcpyDeviceToHost, lat->stream));
+    const int64_t nchunk = transfer_chunks(lat, U_aos != nullptr, E_aos != nullptr);
+    CK(cudaEventRecord(lat->ev[0], lat->stream));
+    for (int i = 0; i < 2; ++i) CK(cudaStreamWaitEvent(lat->side[i], lat->ev[0], 0));
+    for (int64_t k = 0; k < nchunk; ++k) {
+        const int64_t s0 = V * k / nchunk, s1 = V * (k + 1) / nchunk;
+        cudaStream_t st = lat->side[k & 1];
+        DISPATCH(lat->fmt, CK(L::to_aos(lat->g, lat->U[lat->cur], lat->E, U_aos ? du : nullptr,
+                                        E_aos ? de : nullptr, st, s0, s1 - s0)));
+        if (U_aos)
+            CK(cudaMemcpyAsync(U_aos + 3 * nmd * s0, du + 3 * nmd * s0, sizeof(double) * 3 * nmd * (s1 - s0),
+                               cudaMemcpyDeviceToHost, st));
+        if (E_aos)
+            CK(cudaMemcpyAsync(E_aos + 3 * na * s0, de + 3 * na * s0, sizeof(double) * 3 * na * (s1 - s0),
+                               cudaMemcpyDeviceToHost, st));
+    }
+    CK(join_side(lat));
     CK(cudaStreamSynchronize(lat->stream));
     return TCYM_OK;
 }

@@ -42,6 +42,8 @@ struct tcym_lattice_s {
     int64_t steps_done = 0;
     tcym::Tile tile{};   // block tiling of the paired step
     bool tile_chosen = false;
+    cudaStream_t side[2] = {nullptr, nullptr};  // pipelined host transfers (created with the staging)
+    cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
 };
 
 void tcym_set_error(tcym_ctx ctx, const char *fmt, ...);

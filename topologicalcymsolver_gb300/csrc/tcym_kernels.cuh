@@ -51,7 +51,7 @@ constexpr int kThreadsPair = 128;
 #define TCYM_PAIR_SEAM_SPLIT 1
 #endif
 #ifndef TCYM_SU3_PAIR_MINBLOCKS
-#define TCYM_SU3_PAIR_MINBLOCKS 2
+#define TCYM_SU3_PAIR_MINBLOCKS 3
 #endif
 #ifndef TCYM_SU2_PAIR_MINBLOCKS
 #define TCYM_SU2_PAIR_MINBLOCKS 6
@@ -226,13 +226,16 @@ __global__ void k_geodesic(Geom g, const void *Uold, const void *Unew, double c,
     int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (s < g.V) site_geodesic<Fmt<FMT>>(g, Uold, Unew, c, Umid, Emid, s);
 }
-template <int FMT> __global__ void k_from_aos(Geom g, void *U, void *E, const double *Ua, const double *Ea) {
-    int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (s < g.V) site_from_aos<Fmt<FMT>>(g, U, E, Ua, Ea, s);
+// sites [s0, s0 + n) between the reference's AoS FP64 arrays and the device layout
+template <int FMT>
+__global__ void k_from_aos(Geom g, void *U, void *E, const double *Ua, const double *Ea, int64_t s0, int64_t n) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) site_from_aos<Fmt<FMT>>(g, U, E, Ua, Ea, s0 + i);
 }
-template <int FMT> __global__ void k_to_aos(Geom g, const void *U, const void *E, double *Ua, double *Ea) {
-    int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (s < g.V) site_to_aos<Fmt<FMT>>(g, U, E, Ua, Ea, s);
+template <int FMT>
+__global__ void k_to_aos(Geom g, const void *U, const void *E, double *Ua, double *Ea, int64_t s0, int64_t n) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) site_to_aos<Fmt<FMT>>(g, U, E, Ua, Ea, s0 + i);
 }
 
 // ------------------------------------------------------------------ launchers
@@ -305,12 +308,17 @@ template <int FMT> struct Launch {
         k_reunitarize<FMT><<<grid_for(g.V, 128), 128, 0, st>>>(g, U);
         return cudaGetLastError();
     }
-    static cudaError_t from_aos(const Geom &g, void *U, void *E, const double *Ua, const double *Ea, cudaStream_t st) {
-        k_from_aos<FMT><<<grid_for(g.V, 128), 128, 0, st>>>(g, U, E, Ua, Ea);
+    // sites [s0, s0 + n) (n < 0: all)
+    static cudaError_t from_aos(const Geom &g, void *U, void *E, const double *Ua, const double *Ea, cudaStream_t st,
+                                int64_t s0 = 0, int64_t n = -1) {
+        if (n < 0) n = g.V - s0;
+        k_from_aos<FMT><<<grid_for(n, 128), 128, 0, st>>>(g, U, E, Ua, Ea, s0, n);
         return cudaGetLastError();
     }
-    static cudaError_t to_aos(const Geom &g, const void *U, const void *E, double *Ua, double *Ea, cudaStream_t st) {
-        k_to_aos<FMT><<<grid_for(g.V, 128), 128, 0, st>>>(g, U, E, Ua, Ea);
+    static cudaError_t to_aos(const Geom &g, const void *U, const void *E, double *Ua, double *Ea, cudaStream_t st,
+                              int64_t s0 = 0, int64_t n = -1) {
+        if (n < 0) n = g.V - s0;
+        k_to_aos<FMT><<<grid_for(n, 128), 128, 0, st>>>(g, U, E, Ua, Ea, s0, n);
         return cudaGetLastError();
     }
 };

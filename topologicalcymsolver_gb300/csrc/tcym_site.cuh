@@ -108,7 +108,7 @@ TCYM_HD void site_step(const Geom &g, const void *Uin, void *Uout, void *E, cons
 #endif
 constexpr int kPairStapleUnroll = TCYM_PAIR_STAPLE_UNROLL;
 #ifndef TCYM_PAIR_LATE_LOADS
-#define TCYM_PAIR_LATE_LOADS 0
+#define TCYM_PAIR_LATE_LOADS 1
 #endif  // 1: one copy of the staple code for both planes
 // site_step for both sites of pair p of an FP32 lattice with even nz, (x,y,z)
 // and (x,y,z+nz/2), in packed FP32 (f2): the same staples, projection, E
