@@ -170,3 +170,26 @@ def test_energy_drift_fp32_vs_fp64(ctx):
         assert abs(x[100:].mean() - x[:100].mean()) / x.mean() < 2e-4
     assert abs(e32.mean() - e64.mean()) / e64.mean() < 2e-4
     assert l32.observables().unit_max < 1e-5  # periodic FP64 reunitarisation keeps FP32 links on the group
+
+
+@pytest.mark.parametrize("prec,tol", [(tcym.FP64, 1e-9), (tcym.FP32, 1e-4)])
+def test_config2_cooled_ncs_series(ctx, oracle_port, prec, tol):
+    """Config 2's cooled N_CS: Delta N_CS accumulated along the gradient flow as
+    GradientFlow::CalibrationUpdate does (GradientFlow.cpp:168-188, improved E.B),
+    every 10 steps of dtau 0.02, against the oracle (32^3, from the leapfrogged state)."""
+    P = oracle_port[2]
+    shape = (32, 32, 32)
+    src = _cooling_input(ctx, shape, 200)
+    U, E = src.download()
+    lat = tcym.Lattice(ctx, 2, shape, prec)
+    lat.copy_from(src)
+    if prec == tcym.FP32:
+        U, E = lat.download()
+    got, ref = 0.0, 0.0
+    scale = 0.0
+    for _ in range(5):
+        d = lat.flow(0.02, 10, tcym.FLOW_SIMULTANEOUS, calibrate=tcym.NCS_IMPROVED)
+        r = P.flow(shape, U, E, 0.02, 10, 1)
+        got, ref = got + d, ref + r
+        scale = max(scale, abs(r))
+        assert abs(got - ref) <= tol * max(scale, 1e-6), (got, ref)

@@ -88,12 +88,21 @@ __global__ void __launch_bounds__(threads_for<FMT>(), min_blocks_for<FMT>()) k_s
 
 // one thread per site pair (FP32 formats, even nz); blocks touching the seam
 // take the lane-swapping loads
-template <int FMT>
+// TILED = false: the linear mapping, compiled apart so its index arithmetic
+// stays as light as the kernel's register budget wants
+template <int FMT, bool TILED>
 __global__ void __launch_bounds__(kThreadsPair, pair_min_blocks_for<FMT>())
     k_step_pair(Geom g, const void *Uin, void *Uout, void *E, StepCoef<float> c, Tile t) {
     int64_t p;
     bool seam;
-    if (!tile_pair(g, t, blockIdx.x, threadIdx.x, p, seam)) return;
+    if constexpr (TILED) {
+        if (!tile_pair(g, t, blockIdx.x, threadIdx.x, p, seam)) return;
+    } else {
+        const int64_t p0 = (int64_t)blockIdx.x * kThreadsPair;
+        p = p0 + threadIdx.x;
+        if (p >= (g.V >> 1)) return;
+        seam = pairs_touch_seam(g, p0, kThreadsPair);
+    }
 #if TCYM_PAIR_SEAM_SPLIT
     if (seam) site_step_pair<Fmt<FMT>, true>(g, Uin, Uout, E, c, p);
     else site_step_pair<Fmt<FMT>, false>(g, Uin, Uout, E, c, p);
@@ -250,7 +259,9 @@ template <int FMT> struct Launch {
         StepCoef<T> c = coef_cast<T>(cd);
         if constexpr (F::PAIRED) {
             if (doE && doU && g.nz % 2 == 0) {
-                k_step_pair<FMT><<<(unsigned)tile_blocks(g, t), kThreadsPair, 0, st>>>(g, Uin, Uout, E, c, t);
+                const unsigned blocks = (unsigned)tile_blocks(g, t);
+                if (t.tx) k_step_pair<FMT, true><<<blocks, kThreadsPair, 0, st>>>(g, Uin, Uout, E, c, t);
+                else k_step_pair<FMT, false><<<blocks, kThreadsPair, 0, st>>>(g, Uin, Uout, E, c, t);
                 return cudaGetLastError();
             }
         }

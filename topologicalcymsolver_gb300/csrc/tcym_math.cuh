@@ -23,6 +23,16 @@
 #include <stdint.h>
 
 #define TCYM_HD __host__ __device__ __forceinline__
+// rarely taken paths of the step, compiled out of line so that they do not sit in
+// the instruction stream of the common path (1) or inline like the rest (0)
+#ifndef TCYM_COLD_NOINLINE
+#define TCYM_COLD_NOINLINE 0
+#endif
+#if TCYM_COLD_NOINLINE
+#define TCYM_COLD __host__ __device__ __noinline__
+#else
+#define TCYM_COLD TCYM_HD
+#endif
 
 namespace tcym {
 
@@ -513,7 +523,7 @@ template <class T> struct SU3 {
         return mulu<false, false>(w, u);  // reads rows 0 and 1 of w only
     }
     // packed pairs whose exponent needs scaling: each lane through the scalar path
-    template <class P = T> static TCYM_HD Mat iexp_mul_lanes(P c, const P *e, const Mat &u) {
+    template <class P = T> static TCYM_COLD Mat iexp_mul_lanes(P c, const P *e, const Mat &u) {
         Mat r;
 #pragma unroll
         for (int l = 0; l < 2; ++l) {

@@ -139,6 +139,18 @@ TCYM_HD typename F::Mat2 staple_sum_pair(const void *U, int64_t Vh, const PairNb
     return A;
 }
 
+// E += fc f - damp E + kick xi for both sites of pair p (Philox noise of sites p, p + Vh)
+template <int NA>
+TCYM_COLD void langevin_kick_pair(const StepCoef<float> &c, int mu, int64_t p, int64_t Vh, uint64_t step_add, f2 fc,
+                                  const f2 *f, f2 *e) {
+    float x0[NA], x1[NA];
+    normals<float, NA>(c.seed, STREAM_NOISE, c.step + step_add, (uint32_t)p, (uint32_t)mu, x0);
+    normals<float, NA>(c.seed, STREAM_NOISE, c.step + step_add, (uint32_t)(p + Vh), (uint32_t)mu, x1);
+    const f2 damp(sel3(c.damp, mu)), kick(sel3(c.kick, mu));
+#pragma unroll
+    for (int a = 0; a < NA; ++a) e[a] = e[a] + fma(kick, f2(x0[a], x1[a]), fma(-damp, e[a], fc * f[a]));
+}
+
 template <class F, bool SEAM>
 TCYM_HD void site_step_pair(const Geom &g, const void *Uin, void *Uout, void *E, const StepCoef<float> &c, int64_t p,
                             uint64_t step_add = 0) {
@@ -166,12 +178,7 @@ TCYM_HD void site_step_pair(const Geom &g, const void *Uin, void *Uout, void *E,
         G2::proj_mul(u, A, f);
         const f2 fc(sel3(c.fc, mu));
         if (c.mode == MODE_LANGEVIN) {
-            float x0[NA], x1[NA];
-            normals<float, NA>(c.seed, STREAM_NOISE, c.step + step_add, (uint32_t)p, (uint32_t)mu, x0);
-            normals<float, NA>(c.seed, STREAM_NOISE, c.step + step_add, (uint32_t)(p + Vh), (uint32_t)mu, x1);
-            const f2 damp(sel3(c.damp, mu)), kick(sel3(c.kick, mu));
-#pragma unroll
-            for (int a = 0; a < NA; ++a) e[a] = e[a] + fma(kick, f2(x0[a], x1[a]), fma(-damp, e[a], fc * f[a]));
+            langevin_kick_pair<NA>(c, mu, p, Vh, step_add, fc, f, e);
         } else if (c.mode == MODE_FLOW) {
 #pragma unroll
             for (int a = 0; a < NA; ++a) e[a] = fc * f[a];
