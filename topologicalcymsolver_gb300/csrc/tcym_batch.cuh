@@ -44,7 +44,9 @@ __device__ __forceinline__ int find_member(const Member<T> *m, int n, int item, 
 }
 
 // Step k of a chunk for every member: reads U[cur ^ (k&1)], writes U[cur ^ (k&1) ^ 1].
-template <int FMT>
+// GENERAL = false is the lean kernel for the common case of a paired format whose
+// members all take pairs with the linear mapping; true handles every member kind.
+template <int FMT, bool GENERAL>
 __global__ void __launch_bounds__(threads_for<FMT>(), batch_min_blocks_for<FMT>())
     k_step_batch(const Member<typename Fmt<FMT>::T> *__restrict__ members, int nmembers, int total_blocks, int k) {
     static_assert(!Fmt<FMT>::PAIRED || threads_for<FMT>() == kThreadsPair, "one block shape for both paths");
@@ -55,6 +57,17 @@ __global__ void __launch_bounds__(threads_for<FMT>(), batch_min_blocks_for<FMT>(
         // than held in registers for the whole step
         const Member<typename Fmt<FMT>::T> &m = members[mi];
         const Geom g = m.g;
+        if constexpr (Fmt<FMT>::PAIRED && !GENERAL) {
+            const int64_t p0 = (int64_t)(item - m.block_begin) * kThreadsPair, p = p0 + threadIdx.x;
+            if (p < (g.V >> 1)) {
+                const int in = m.cur ^ (k & 1);
+                if (pairs_touch_seam(g, p0, kThreadsPair))
+                    site_step_pair<Fmt<FMT>, true>(g, m.U[in], m.U[in ^ 1], m.E, m.c, p, (uint64_t)k);
+                else
+                    site_step_pair<Fmt<FMT>, false>(g, m.U[in], m.U[in ^ 1], m.E, m.c, p, (uint64_t)k);
+            }
+            continue;
+        }
         if constexpr (Fmt<FMT>::PAIRED) {
             if (m.paired) {  // block-uniform
                 int64_t p;
@@ -127,11 +140,14 @@ template <int FMT> struct LaunchBatch {
     static constexpr int TPB = threads_for<FMT>();
     static int resident_blocks() {
         int b = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_step_batch<FMT>, TPB, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_step_batch<FMT, true>, TPB, 0);
         return b > 0 ? b : 1;
     }
-    static cudaError_t step(const Member<T> *members, int n, int total_blocks, int k, int grid, cudaStream_t st) {
-        k_step_batch<FMT><<<grid, TPB, 0, st>>>(members, n, total_blocks, k);
+    // general: some member is unpaired or tiled (see k_step_batch)
+    static cudaError_t step(const Member<T> *members, int n, int total_blocks, int k, int grid, bool general,
+                            cudaStream_t st) {
+        if (general || !Fmt<FMT>::PAIRED) k_step_batch<FMT, true><<<grid, TPB, 0, st>>>(members, n, total_blocks, k);
+        else k_step_batch<FMT, false><<<grid, TPB, 0, st>>>(members, n, total_blocks, k);
         return cudaGetLastError();
     }
     static cudaError_t observables(const Member<T> *members, int n, int total_blocks, int mask, double *partial,

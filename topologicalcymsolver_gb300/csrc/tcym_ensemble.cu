@@ -45,6 +45,7 @@ struct FmtGroup {
     size_t d_bytes = 0;
     std::vector<char> h_members; // host copy of the table
     int total_blocks = 0, red_total = 0, grid = 0, red_grid = 0, red_offset = 0;
+    bool general = false;        // some member is unpaired or tiled: the general batch kernel
 };
 
 int fail(tcym_ctx ctx, cudaError_t e, const char *w) {
@@ -81,6 +82,7 @@ template <int FMT> static void fill_group(tcym_ensemble ens, FmtGroup &G, int sm
     constexpr int TPB = threads_for<FMT>();
     std::vector<Member<T>> tab(G.idx.size());
     int blk = 0, red = 0;
+    G.general = false;
     for (size_t i = 0; i < G.idx.size(); ++i) {
         const EnsMember &em = ens->members[G.idx[i]];
         const tcym_lattice L = em.lat;
@@ -95,6 +97,7 @@ template <int FMT> static void fill_group(tcym_ensemble ens, FmtGroup &G, int sm
         m.block_begin = blk;
         m.paired = Fmt<FMT>::PAIRED && L->g.nz % 2 == 0;
         m.tile = m.paired ? tcym_lattice_tile_of(L) : Tile{0, 0, 0, 0, 0};
+        if (!m.paired || m.tile.tx != 0) G.general = true;
         blk += m.paired ? (int)tile_blocks(L->g, m.tile) : grid_for(L->g.V, TPB);
         m.red_begin = red;
         m.red_blocks = grid_for(L->g.V, kRedThreads);
@@ -174,7 +177,7 @@ template <int FMT> static cudaError_t launch_group_step(tcym_ensemble ens, int f
     using T = typename Fmt<FMT>::T;
     const FmtGroup &G = ens->groups[f];
     return LaunchBatch<FMT>::step(static_cast<const Member<T> *>(G.d_members), (int)G.idx.size(), G.total_blocks, k,
-                                  G.grid, s);
+                                  G.grid, G.general, s);
 }
 
 static cudaError_t group_step(tcym_ensemble ens, int f, int k, cudaStream_t s) {
