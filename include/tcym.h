@@ -206,7 +206,9 @@ int tcym_gauss_restore(tcym_lattice lat, double tol, int maxit, int *iters, doub
  * the library until the process exits.  Lattices whose violation array (NA * V doubles)
  * exceeds 1,036,272 doubles are rejected with TCYM_ERR_ARG: SU(2) at most 345,424 sites,
  * SU(3) at most 129,534 sites.
- * The first call on a device looks up the scratch address for that device (once); make
+ * The first call on a device looks up the scratch address for that device and loads the
+ * code of the kernels it runs, for both groups (once; with lazy module loading the runtime
+ * would otherwise place each kernel's code in device memory at its first launch); make
  * that first call before any stream capture.  All calls share the one scratch array,
  * which keeps the last call's contents (each call clears what must start at zero): calls
  * that overlap on the GPU, from any thread or stream, race and must not be issued. */

@@ -235,16 +235,49 @@ __global__ void k_geodesic(Geom g, const void *Uold, const void *Unew, double c,
     int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (s < g.V) site_geodesic<Fmt<FMT>>(g, Uold, Unew, c, Umid, Emid, s);
 }
-// sites [s0, s0 + n) between the reference's AoS FP64 arrays and the device layout
-template <int FMT>
-__global__ void k_from_aos(Geom g, void *U, void *E, const double *Ua, const double *Ea, int64_t s0, int64_t n) {
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) site_from_aos<Fmt<FMT>>(g, U, E, Ua, Ea, s0 + i);
+// Sites [s0, s0 + n) between the reference's AoS FP64 arrays and the device
+// layout.  A block takes kAosSites sites: their AoS records (SU(3): 432 + 192 B a
+// site) pass through shared memory, so that the AoS side is read or written by
+// consecutive threads at consecutive addresses; each thread then converts one link.
+constexpr int kAosSites = 64, kAosThreads = 192;
+template <int FMT> constexpr int aos_link_doubles() { return Fmt<FMT>::NA == 3 ? 4 : 18; }
+template <int FMT> constexpr size_t aos_smem() {
+    return sizeof(double) * kAosSites * 3 * (aos_link_doubles<FMT>() + Fmt<FMT>::NA);
 }
 template <int FMT>
-__global__ void k_to_aos(Geom g, const void *U, const void *E, double *Ua, double *Ea, int64_t s0, int64_t n) {
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) site_to_aos<Fmt<FMT>>(g, U, E, Ua, Ea, s0 + i);
+__global__ void __launch_bounds__(kAosThreads)
+    k_from_aos(Geom g, void *U, void *E, const double *Ua, const double *Ea, int64_t s0, int64_t n) {
+    using F = Fmt<FMT>;
+    constexpr int NMD = aos_link_doubles<FMT>(), NA = F::NA;
+    extern __shared__ double aos_sh[];
+    double *su = aos_sh, *se = aos_sh + kAosSites * 3 * NMD;
+    const int64_t b0 = s0 + (int64_t)blockIdx.x * kAosSites;
+    const int ns = (int)(n - (b0 - s0) < kAosSites ? n - (b0 - s0) : kAosSites);
+    if (Ua)
+        for (int i = threadIdx.x; i < ns * 3 * NMD; i += blockDim.x) su[i] = Ua[b0 * 3 * NMD + i];
+    if (Ea)
+        for (int i = threadIdx.x; i < ns * 3 * NA; i += blockDim.x) se[i] = Ea[b0 * 3 * NA + i];
+    __syncthreads();
+    const int l = threadIdx.x, site = l / 3, mu = l - 3 * site;
+    if (site >= ns) return;
+    site_link_from_aos<F>(g, U, E, Ua ? su : nullptr, Ea ? se : nullptr, site, b0 + site, mu);
+}
+template <int FMT>
+__global__ void __launch_bounds__(kAosThreads)
+    k_to_aos(Geom g, const void *U, const void *E, double *Ua, double *Ea, int64_t s0, int64_t n) {
+    using F = Fmt<FMT>;
+    constexpr int NMD = aos_link_doubles<FMT>(), NA = F::NA;
+    extern __shared__ double aos_sh[];
+    double *su = aos_sh, *se = aos_sh + kAosSites * 3 * NMD;
+    const int64_t b0 = s0 + (int64_t)blockIdx.x * kAosSites;
+    const int ns = (int)(n - (b0 - s0) < kAosSites ? n - (b0 - s0) : kAosSites);
+    const int l = threadIdx.x, site = l / 3, mu = l - 3 * site;
+    if (site < ns) site_link_to_aos<F>(g, U, E, Ua ? su : nullptr, Ea ? se : nullptr, site, b0 + site, mu);
+    __syncthreads();
+    if (Ua)
+        for (int i = threadIdx.x; i < ns * 3 * NMD; i += blockDim.x) Ua[b0 * 3 * NMD + i] = su[i];
+    if (Ea)
+        for (int i = threadIdx.x; i < ns * 3 * NA; i += blockDim.x) Ea[b0 * 3 * NA + i] = se[i];
 }
 
 // ------------------------------------------------------------------ launchers
@@ -323,13 +356,13 @@ template <int FMT> struct Launch {
     static cudaError_t from_aos(const Geom &g, void *U, void *E, const double *Ua, const double *Ea, cudaStream_t st,
                                 int64_t s0 = 0, int64_t n = -1) {
         if (n < 0) n = g.V - s0;
-        k_from_aos<FMT><<<grid_for(n, 128), 128, 0, st>>>(g, U, E, Ua, Ea, s0, n);
+        k_from_aos<FMT><<<grid_for(n, kAosSites), kAosThreads, aos_smem<FMT>(), st>>>(g, U, E, Ua, Ea, s0, n);
         return cudaGetLastError();
     }
     static cudaError_t to_aos(const Geom &g, const void *U, const void *E, double *Ua, double *Ea, cudaStream_t st,
                               int64_t s0 = 0, int64_t n = -1) {
         if (n < 0) n = g.V - s0;
-        k_to_aos<FMT><<<grid_for(n, 128), 128, 0, st>>>(g, U, E, Ua, Ea, s0, n);
+        k_to_aos<FMT><<<grid_for(n, kAosSites), kAosThreads, aos_smem<FMT>(), st>>>(g, U, E, Ua, Ea, s0, n);
         return cudaGetLastError();
     }
 };
@@ -338,5 +371,7 @@ template <int FMT> struct Launch {
 // advance the Kahan-compensated N_CS by ncs_dt * E.B / (8 pi^2).
 cudaError_t finalize_obs(const double *partial, int blocks, int na, int64_t V, double ncs_dt, double *result,
                          cudaStream_t st);
+// loads k_finalize's code now (with lazy module loading it would load at its first launch)
+cudaError_t preload_finalize();
 
 }  // namespace tcym

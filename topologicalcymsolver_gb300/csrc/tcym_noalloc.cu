@@ -81,6 +81,9 @@ static __device__ __align__(256) double g_noalloc_scratch[kNoAllocScratchDoubles
 
 // Device address of g_noalloc_scratch for each device, looked up once per
 // device with that device current (host code may not use the symbol itself).
+// The same first call loads every kernel the entry point runs, for both groups:
+// with lazy module loading the runtime would otherwise place a kernel's code in
+// device memory at its first launch, i.e. inside a later call.
 static std::mutex g_scratch_mu;
 static double *g_scratch_addr[256];
 
@@ -91,6 +94,13 @@ static cudaError_t scratch_address(int dev, double **out) {
         void *p = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess) return e;
+        cudaFuncAttributes fa;
+        if ((e = cudaFuncGetAttributes(&fa, k_gauss_compute<FMT_SU2_AOS64>)) != cudaSuccess ||
+            (e = cudaFuncGetAttributes(&fa, k_gauss_compute<FMT_SU3_AOS64>)) != cudaSuccess ||
+            (e = cudaFuncGetAttributes(&fa, k_gauss_update<FMT_SU2_AOS64>)) != cudaSuccess ||
+            (e = cudaFuncGetAttributes(&fa, k_gauss_update<FMT_SU3_AOS64>)) != cudaSuccess ||
+            (e = preload_finalize()) != cudaSuccess)
+            return e;
         g_scratch_addr[dev] = static_cast<double *>(p);
     }
     *out = g_scratch_addr[dev];

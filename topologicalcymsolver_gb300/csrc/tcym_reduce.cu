@@ -59,6 +59,11 @@ __global__ void __launch_bounds__(kRedThreads) k_finalize(const double *partial,
     finalize_block(partial, blocks, na, V, ncs_dt, res, nullptr, nullptr);
 }
 
+cudaError_t preload_finalize() {
+    cudaFuncAttributes fa;
+    return cudaFuncGetAttributes(&fa, k_finalize);
+}
+
 cudaError_t finalize_obs(const double *partial, int blocks, int na, int64_t V, double ncs_dt, double *result,
                          cudaStream_t st) {
     k_finalize<<<1, kRedThreads, 0, st>>>(partial, blocks, na, V, ncs_dt, result);

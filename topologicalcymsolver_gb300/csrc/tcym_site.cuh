@@ -587,6 +587,55 @@ template <class F> TCYM_HD void site_from_aos(const Geom &g, void *U, void *E, c
     }
 }
 
+// One link (mu) of site s from / to AoS records held at slot k of a staging area
+// (the AoS arrays themselves when k = s), for the shared-memory conversion kernels.
+template <class F>
+TCYM_HD void site_link_from_aos(const Geom &g, void *U, void *E, const double *Ua, const double *Ea, int64_t k,
+                                int64_t s, int mu) {
+    using T = typename F::T;
+    constexpr int NMD = F::NA == 3 ? 4 : 18;
+    if (Ua) {
+        typename F::Mat m;
+        const double *a = Ua + NMD * (mu + 3 * k);
+        if constexpr (F::NA == 3) {
+            for (int q = 0; q < 4; ++q) m.q[q] = (T)a[q];
+        } else {
+            for (int i = 0; i < 3; ++i)
+                for (int j = 0; j < 3; ++j) m.m[i][j] = cx<T>{(T)a[2 * (i + 3 * j)], (T)a[2 * (i + 3 * j) + 1]};
+        }
+        F::store(U, g.V, mu, s, m);
+    }
+    if (Ea) {
+        T e[F::NA];
+        for (int a = 0; a < F::NA; ++a) e[a] = (T)Ea[F::NA * (mu + 3 * k) + a];
+        F::store_e(E, g.V, mu, s, e);
+    }
+}
+template <class F>
+TCYM_HD void site_link_to_aos(const Geom &g, const void *U, const void *E, double *Ua, double *Ea, int64_t k,
+                              int64_t s, int mu) {
+    using T = typename F::T;
+    constexpr int NMD = F::NA == 3 ? 4 : 18;
+    if (Ua) {
+        const typename F::Mat m = F::load(U, g.V, mu, s);
+        double *a = Ua + NMD * (mu + 3 * k);
+        if constexpr (F::NA == 3) {
+            for (int q = 0; q < 4; ++q) a[q] = (double)m.q[q];
+        } else {
+            for (int i = 0; i < 3; ++i)
+                for (int j = 0; j < 3; ++j) {
+                    a[2 * (i + 3 * j)] = (double)m.m[i][j].re;
+                    a[2 * (i + 3 * j) + 1] = (double)m.m[i][j].im;
+                }
+        }
+    }
+    if (Ea) {
+        T e[F::NA];
+        F::load_e(E, g.V, mu, s, e);
+        for (int a = 0; a < F::NA; ++a) Ea[F::NA * (mu + 3 * k) + a] = (double)e[a];
+    }
+}
+
 template <class F> TCYM_HD void site_to_aos(const Geom &g, const void *U, const void *E, double *Ua, double *Ea, int64_t s) {
     using T = typename F::T;
     constexpr int NMD = F::NA == 3 ? 4 : 18;
