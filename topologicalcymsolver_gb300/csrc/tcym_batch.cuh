@@ -170,7 +170,7 @@ cudaError_t finalize_members(const MemberReduce *items, int n, double *out, cuda
 
 }  // namespace tcym
 
-// The kernels are instantiated once, in tcym_kern_su2.cu and tcym_kern_su3.cu
+// The kernels are instantiated once, in the tcym_kern_su{2,3}_f{32,64}*.cu units
 // (which define TCYM_KERNEL_TU); every other unit only refers to them.
 #ifndef TCYM_KERNEL_TU
 namespace tcym {
