@@ -56,16 +56,6 @@ constexpr int kThreadsPair = 128;
 #ifndef TCYM_SU2_PAIR_MINBLOCKS
 #define TCYM_SU2_PAIR_MINBLOCKS 6
 #endif
-// the paired step's buffers never alias (links ping-pong, fields apart): __restrict__
-// lets the compiler read the links through the read-only path and reorder the loads
-#ifndef TCYM_PAIR_RESTRICT_ON
-#define TCYM_PAIR_RESTRICT_ON 0
-#endif
-#if TCYM_PAIR_RESTRICT_ON
-#define TCYM_PAIR_RESTRICT __restrict__
-#else
-#define TCYM_PAIR_RESTRICT
-#endif
 template <int FMT> constexpr int pair_min_blocks_for() {
     return Fmt<FMT>::NA == 8 ? TCYM_SU3_PAIR_MINBLOCKS : TCYM_SU2_PAIR_MINBLOCKS;
 }
@@ -102,8 +92,7 @@ __global__ void __launch_bounds__(threads_for<FMT>(), min_blocks_for<FMT>()) k_s
 // stays as light as the kernel's register budget wants
 template <int FMT, bool TILED>
 __global__ void __launch_bounds__(kThreadsPair, pair_min_blocks_for<FMT>())
-    k_step_pair(Geom g, const void *TCYM_PAIR_RESTRICT Uin, void *TCYM_PAIR_RESTRICT Uout,
-                void *TCYM_PAIR_RESTRICT E, StepCoef<float> c, Tile t) {
+    k_step_pair(Geom g, const void *Uin, void *Uout, void *E, StepCoef<float> c, Tile t) {
     int64_t p;
     bool seam;
     if constexpr (TILED) {
