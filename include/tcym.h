@@ -111,6 +111,14 @@ int tcym_lattice_bytes(tcym_lattice lat, size_t *bytes);
 int tcym_lattice_upload(tcym_lattice lat, const double *U_aos, const double *E_aos);
 /* Copies the state out to host AoS FP64 arrays (either may be NULL). */
 int tcym_lattice_download(tcym_lattice lat, double *U_aos, double *E_aos);
+/* One leapfrog step (Dynamics::Update, DYNAMICS/Dynamics.cpp:204-218) of a state held in host memory:
+ * U_in/E_in in, U_out/E_out out, in the AoS layouts of tcym_lattice_upload (U_out may be U_in, E_out
+ * E_in).  The upload, the step and the download run as one pipeline over z-ordered chunks, so both
+ * transfer directions overlap each other and the step; the lattice holds the new state afterwards,
+ * as after tcym_lattice_upload + tcym_leapfrog(lat, dt, 1) + tcym_lattice_download, bit for bit.
+ * Host buffers in pinned memory (cudaMallocHost / cudaHostRegister) make the copies asynchronous. */
+int tcym_leapfrog_host(tcym_lattice lat, double dt, const double *U_in, const double *E_in, double *U_out,
+                       double *E_out);
 /* dst <- src (same group and extents; any precisions): Copy() of GaugeLinks.cpp:91-107
  * and ElectricFields.cpp:90-104. */
 int tcym_lattice_copy(tcym_lattice dst, const tcym_lattice src);

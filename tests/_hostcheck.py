@@ -40,6 +40,8 @@ def load():
         L.hc_normal.argtypes = [ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32,
                                 ctypes.c_uint32, ctypes.c_int]
         L.hc_normal.restype = ctypes.c_double
+        L.hc_pipeline_schedule.argtypes = [ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, _vp, _vp, ctypes.c_int64]
+        L.hc_pipeline_schedule.restype = ctypes.c_int64
         _L = L
     return _L
 
@@ -135,3 +137,13 @@ def ilog(nc, prec, c, v):
 
 def normal(seed, stream, step, site, mu, a, single=False):
     return load().hc_normal(seed, stream, step, site, mu, a, int(single))
+
+
+def pipeline_schedule(N, P, C):
+    """[(kind, chunk)] of the host-resident step's pipeline (0 upload, 1 step)."""
+    L = load()
+    cap = 4 * ((N + C - 1) // C) + 4
+    kinds, chunks = np.zeros(cap, np.int32), np.zeros(cap, np.int64)
+    n = L.hc_pipeline_schedule(N, P, C, _p(kinds), _p(chunks), cap)
+    assert n <= cap
+    return list(zip(kinds[:n].tolist(), chunks[:n].tolist()))

@@ -193,6 +193,29 @@ def test_upload_download_roundtrip(ctx, oracle_port, nc):
 
 
 @pytest.mark.parametrize("nc", GROUPS)
+@pytest.mark.parametrize("shape", [(4, 6, 6), (3, 5, 7)])  # even volume; odd volume (a padded last pair)
+def test_reunitarize_fp32_vs_fp64(ctx, oracle_port, nc, shape):
+    """Links drifted off the group: the FP64 lattice's Gram-Schmidt puts them on
+    the group to 1e-14; the FP32 lattice's (FP64 arithmetic on the FP32 links)
+    agrees with it to a few FP32 ulps and is on the group to FP32 rounding."""
+    P = oracle_port[nc]
+    U, E = random_state(P, nc, shape)
+    U = U * (1 + 1e-3 * np.random.default_rng(4).normal(size=U.shape))
+    lat64 = tcym.Lattice(ctx, nc, shape, tcym.FP64)
+    lat32 = tcym.Lattice(ctx, nc, shape, tcym.FP32)
+    lat64.upload(U, E)
+    lat32.upload(U, E)
+    assert lat32.observables().unit_max > 1e-4
+    lat64.reunitarize()
+    lat32.reunitarize()
+    assert lat64.observables().unit_max < 1e-14
+    assert lat32.observables().unit_max < 1e-6
+    U64, _ = lat64.download()
+    U32, _ = lat32.download()
+    assert np.abs(U32 - U64).max() < 3e-7
+
+
+@pytest.mark.parametrize("nc", GROUPS)
 def test_ncs_tracking_is_kahan_sum_of_edotb(ctx, oracle_port, nc):
     shape = (6, 6, 6)
     P = oracle_port[nc]

@@ -1,0 +1,66 @@
+"""The issue order of the host-resident step (tcym_leapfrog_host) on the CPU:
+the library's own schedule, through the host check build, checked for every
+chunk's whole stencil being on the device before the chunk is stepped.
+
+Storage units are sites, or the site pairs (x, y, z) + (x, y, z + nz/2) of the
+paired FP32 step; either way unit (x, y, z') has index x + nx (y + ny z') with
+z' < nz' (nz, or nz/2 for pairs), and its stencil lies in the 3 x 3 x 3 block
+around it, periodic in all three directions (for pairs, the wrap in z' is the
+seam where neighbours arrive lane-swapped).
+"""
+import numpy as np
+import pytest
+
+from tests import _hostcheck as hc
+
+
+def stencil_max(nx, ny, nzp, a, b):
+    """Largest index in the 3x3x3 periodic neighbourhood of units [a, b)."""
+    i = np.arange(a, b)
+    x, y, z = i % nx, (i // nx) % ny, i // (nx * ny)
+    m = -1
+    for dz in (-1, 0, 1):
+        for dy in (-1, 0, 1):
+            for dx in (-1, 0, 1):
+                j = (x + dx) % nx + nx * ((y + dy) % ny + ny * ((z + dz) % nzp))
+                m = max(m, int(j.max()))
+    return m
+
+
+def check_schedule(nx, ny, nzp, C):
+    N, P = nx * ny * nzp, nx * ny
+    ops = hc.pipeline_schedule(N, P, C)
+    n = (N + C - 1) // C
+    assert sorted(j for k, j in ops if k == 0) == list(range(n))
+    assert sorted(j for k, j in ops if k == 1) == list(range(n))
+    up = 0  # uploads are in chunk order, so the units on the device are [0, up)
+    expect_next = 0
+    for kind, j in ops:
+        a, b = j * C, min(N, (j + 1) * C)
+        if kind == 0:
+            assert j == expect_next
+            expect_next += 1
+            up = b
+            continue
+        assert stencil_max(nx, ny, nzp, a, b) < up, (nx, ny, nzp, C, j, up)
+    return ops
+
+
+@pytest.mark.parametrize("nx,ny,nz", [(8, 8, 12), (8, 8, 9), (16, 16, 8), (12, 10, 14), (5, 6, 7), (128, 128, 128),
+                                      (2, 2, 2), (96, 96, 96)])
+@pytest.mark.parametrize("paired", [True, False])
+@pytest.mark.parametrize("C", [128, 256, 1024, 13440, 53760, 1 << 20])
+def test_schedule_respects_neighbourhoods(nx, ny, nz, paired, C):
+    if paired and nz % 2:
+        pytest.skip("the paired step needs an even nz")
+    check_schedule(nx, ny, nz // 2 if paired else nz, C)
+
+
+def test_schedule_overlaps_steps_with_uploads():
+    """At 128^3 (paired, 64 MB chunks) steps start long before the last upload:
+    the transfer directions overlap."""
+    ops = check_schedule(128, 128, 64, 53760)
+    first_step = next(i for i, (k, _) in enumerate(ops) if k == 1)
+    last_upload = max(i for i, (k, _) in enumerate(ops) if k == 0)
+    n = (128 ** 3 // 2 + 53759) // 53760
+    assert first_step < 6 and last_upload > n  # stepping starts within the first few uploads

@@ -166,6 +166,27 @@ def test_reunitarize_restores_group(oracle_port, nc):
 
 
 @pytest.mark.parametrize("nc", [2, 3])
+@pytest.mark.parametrize("shape", [(3, 3, 4), (3, 3, 3)])  # even volume; odd volume (a padded pair)
+def test_fp32_reunitarize_matches_fp64(oracle_port, nc, shape):
+    """FP32 links are widened to FP64, projected and rounded back: the FP64
+    lattice's result to a few FP32 ulps (the input was rounded to FP32 first,
+    and row 2 of SU(3) is rebuilt in FP32), on the group to FP32 rounding."""
+    P = oracle_port[nc]
+    U, E = _state(P, nc, shape, 22)
+    U = U * (1 + 1e-3 * np.random.default_rng(2).normal(size=U.shape))
+    H32, H64 = hc.HostLattice(nc, "f32", shape), hc.HostLattice(nc, "f64", shape)
+    H32.upload(U, E)
+    H64.upload(U, E)
+    assert H32.observables()[11] > 1e-4
+    H32.reunitarize()
+    H64.reunitarize()
+    assert H32.observables()[11] < 1e-6
+    U32, _ = H32.download()
+    U64, _ = H64.download()
+    assert np.abs(U32 - U64).max() < 3e-7
+
+
+@pytest.mark.parametrize("nc", [2, 3])
 def test_initial_conditions(oracle_port, nc):
     P = oracle_port[nc]
     shape = (3, 4, 5)

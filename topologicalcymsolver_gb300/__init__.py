@@ -114,6 +114,8 @@ def library() -> ctypes.CDLL:
         "tcym_lattice_bytes": ([ctypes.c_void_p, ctypes.POINTER(ctypes.c_size_t)], ctypes.c_int),
         "tcym_lattice_upload": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
         "tcym_lattice_download": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+        "tcym_leapfrog_host": ([ctypes.c_void_p, ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                ctypes.c_void_p], ctypes.c_int),
         "tcym_lattice_copy": ([ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
         "tcym_lattice_sync": ([ctypes.c_void_p], ctypes.c_int),
         "tcym_lattice_stream": ([ctypes.c_void_p, c_void_pp], ctypes.c_int),
@@ -255,6 +257,18 @@ class Lattice:
         E = np.empty((self.V, 3, NA[self.nc])) if E is None else E
         self.ctx.check(self.lib.tcym_lattice_download(self.h, _ptr(U), _ptr(E)))
         return U, E
+
+    def leapfrog_host(self, dt: float, U, E, U_out=None, E_out=None):
+        """One leapfrog step of a state in host memory (reference AoS FP64 arrays):
+        upload, step and download pipelined over z-ordered chunks; returns the new
+        state (U_out, E_out, which may be U and E themselves)."""
+        U_out = np.empty_like(U) if U_out is None else U_out
+        E_out = np.empty_like(E) if E_out is None else E_out
+        for a, n in ((U, NM[self.nc]), (E, NA[self.nc]), (U_out, NM[self.nc]), (E_out, NA[self.nc])):
+            if a.dtype != np.float64 or not a.flags.c_contiguous or a.size != self.V * 3 * n:
+                raise ValueError("leapfrog_host: C-contiguous float64 arrays of the reference AoS shapes expected")
+        self.ctx.check(self.lib.tcym_leapfrog_host(self.h, dt, _ptr(U), _ptr(E), _ptr(U_out), _ptr(E_out)))
+        return U_out, E_out
 
     def copy_from(self, other: "Lattice"):
         self.ctx.check(self.lib.tcym_lattice_copy(self.h, other.h))

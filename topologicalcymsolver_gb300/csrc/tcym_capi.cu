@@ -6,6 +6,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <new>
@@ -14,6 +15,7 @@
 #include "../../include/tcym.h"
 #include "tcym_batch.cuh"
 #include "tcym_internal.h"
+#include "tcym_pipeline.h"
 
 using namespace tcym;
 
@@ -136,9 +138,17 @@ extern "C" const char *tcym_last_error(tcym_ctx ctx) {
 }
 
 // ------------------------------------------------------------------ lattices
+static void drop_host_graphs(tcym_lattice lat) {
+    for (auto &h : lat->host_graph) {
+        if (h.exec) cudaGraphExecDestroy(h.exec);
+        h = tcym_lattice_s::HostStepGraph{};
+    }
+}
+
 static void lattice_free(tcym_lattice lat) {
     cudaSetDevice(lat->ctx->device);
     if (lat->stream) cudaStreamSynchronize(lat->stream);
+    drop_host_graphs(lat);
     cudaFree(lat->U[0]);
     cudaFree(lat->U[1]);
     cudaFree(lat->E);
@@ -151,6 +161,10 @@ static void lattice_free(tcym_lattice lat) {
         if (lat->side[i]) cudaStreamDestroy(lat->side[i]);
     for (int i = 0; i < 3; ++i)
         if (lat->ev[i]) cudaEventDestroy(lat->ev[i]);
+    for (auto &st : lat->hs)
+        if (st) cudaStreamDestroy(st);
+    for (auto &ev : lat->hev)
+        if (ev) cudaEventDestroy(ev);
     if (lat->stream) cudaStreamDestroy(lat->stream);
 }
 
@@ -229,6 +243,7 @@ static int ensure_staging(tcym_lattice lat) {
     for (int i = 0; i < 3; ++i)
         if (!lat->ev[i]) CK(cudaEventCreateWithFlags(&lat->ev[i], cudaEventDisableTiming));
     if (lat->staging_bytes >= need) return TCYM_OK;
+    drop_host_graphs(lat);
     cudaFree(lat->staging);
     lat->staging = nullptr;
     lat->staging_bytes = 0;
@@ -355,6 +370,7 @@ void tcym_lattice_release_scratch(tcym_lattice lat) {
     if (!lat) return;
     cudaSetDevice(lat->ctx->device);
     cudaStreamSynchronize(lat->stream);
+    drop_host_graphs(lat);
     cudaFree(lat->gauss);
     cudaFree(lat->staging);
     lat->gauss = nullptr;
@@ -539,6 +555,169 @@ int tcym_run_steps(tcym_lattice lat, int mode, double dt, double gamma, double T
 extern "C" int tcym_leapfrog(tcym_lattice lat, double dt, int nsteps) {
     if (!lat || nsteps < 0) return TCYM_ERR_ARG;
     return tcym_run_steps(lat, MODE_LEAPFROG, dt, 0, 0, 0, 0, nsteps);
+}
+
+// ------------------------------------------------------ host-resident step
+// The pipeline of tcym_leapfrog_host (order in tcym_pipeline.h) on five
+// streams, so that neither copy stream waits behind a kernel: host-to-device
+// copies of each chunk (hs[0]); their conversion to the storage layout (hs[1]);
+// the step of each chunk on the lattice's stream once its neighbour planes are
+// converted; conversion of the stepped chunk back to AoS (hs[2]); its
+// device-to-host copies (hs[3]).  Host data of a chunk of storage units
+// [a, b): sites [a, b), and for site pairs also their partners [a + Vh,
+// b + Vh), moved as one two-row copy per array.  The staging buffer holds the
+// AoS state; a chunk's region is converted back into only after it was
+// uploaded and converted, so one buffer serves both directions (and U_out
+// may be U_in).  Each event is waited on right after it is recorded, so one
+// event per edge of the chain suffices.
+template <int FMT>
+static cudaError_t host_step_pipeline(tcym_lattice lat, const StepCoef<double> &c, int64_t C, const double *U_in,
+                                      const double *E_in, double *U_out, double *E_out) {
+    using L = Launch<FMT>;
+    const int nmd = lat->nc == 2 ? 4 : 18, na = lat->nc == 2 ? 3 : 8;
+    const Geom &g = lat->g;
+    const int64_t V = g.V, Vh = pair_sites(V), P = (int64_t)g.nx * g.ny;
+    const bool paired = L::paired_step(g);  // then V is even and both halves of a chunk are as long
+    const int64_t N = paired ? Vh : V;
+    double *du = lat->staging, *de = lat->staging + 3 * nmd * V;
+    const void *Uin = lat->U[lat->cur];
+    void *Uout = lat->U[1 - lat->cur];
+    cudaStream_t cin = lat->hs[0], vin = lat->hs[1], vout = lat->hs[2], cout = lat->hs[3], cs = lat->stream;
+    cudaEvent_t *ev = lat->hev;  // 0 start, 1 copied in, 2 converted in, 3 stepped, 4 converted out, 5 joins
+    cudaError_t err = cudaEventRecord(ev[0], cs);
+    for (cudaStream_t st : lat->hs)
+        if (err == cudaSuccess) err = cudaStreamWaitEvent(st, ev[0], 0);
+    // both halves of a chunk in one two-row copy (pitch Vh sites), or one range
+    auto copy = [&](double *dst, const double *src, int64_t a, int64_t n, int nd, cudaMemcpyKind kind,
+                    cudaStream_t st) {
+        if (err != cudaSuccess) return;
+        const size_t w = sizeof(double) * 3 * nd * n, pitch = sizeof(double) * 3 * nd * Vh;
+        if (paired)
+            err = cudaMemcpy2DAsync(dst + 3 * nd * a, pitch, src + 3 * nd * a, pitch, w, 2, kind, st);
+        else
+            err = cudaMemcpyAsync(dst + 3 * nd * a, src + 3 * nd * a, w, kind, st);
+    };
+    auto link = [&](cudaEvent_t e, cudaStream_t from, cudaStream_t to) {
+        if (err == cudaSuccess) err = cudaEventRecord(e, from);
+        if (err == cudaSuccess) err = cudaStreamWaitEvent(to, e, 0);
+    };
+    pipeline_schedule(N, P, C, [&](int op, int64_t j) {
+        if (err != cudaSuccess) return;
+        const int64_t a = j * C, n = ((j + 1) * C < N ? (j + 1) * C : N) - a;
+        if (op == PIPE_UPLOAD) {
+            copy(du, U_in, a, n, nmd, cudaMemcpyHostToDevice, cin);
+            copy(de, E_in, a, n, na, cudaMemcpyHostToDevice, cin);
+            link(ev[1], cin, vin);
+            for (int h = 0; h < (paired ? 2 : 1) && err == cudaSuccess; ++h)
+                err = L::from_aos(g, lat->U[lat->cur], lat->E, du, de, vin, a + h * Vh, n);
+            // the latest conversion covers this chunk's neighbourhood when a step follows
+            link(ev[2], vin, cs);
+        } else {
+            if (err == cudaSuccess) err = L::step_range(g, Uin, Uout, lat->E, c, a, a + n, cs);
+            link(ev[3], cs, vout);
+            for (int h = 0; h < (paired ? 2 : 1) && err == cudaSuccess; ++h)
+                err = L::to_aos(g, Uout, lat->E, du, de, vout, a + h * Vh, n);
+            link(ev[4], vout, cout);
+            copy(U_out, du, a, n, nmd, cudaMemcpyDeviceToHost, cout);
+            copy(E_out, de, a, n, na, cudaMemcpyDeviceToHost, cout);
+        }
+    });
+    // the lattice's stream waits for the last download (which follows every other operation)
+    // and for the other side streams, which are idle by then but must join a capture
+    for (cudaStream_t st : lat->hs) link(ev[5], st, cs);
+    return err;
+}
+
+// Units per chunk of the host-step pipeline: about 64 MB of host data, a
+// multiple of 128 (TCYM_HOST_STEP_CHUNK overrides, in units).  Measured on
+// GB300 at 128^3 SU(3): 8.9 ms per step with 64 MB chunks, 9.5-14 ms with
+// 16 MB and 12 ms with 5 MB (more, smaller copies), against 14.3 ms for the
+// three calls upload, step, download.
+static int64_t host_step_chunk(tcym_lattice lat, bool paired) {
+    const int nmd = lat->nc == 2 ? 4 : 18, na = lat->nc == 2 ? 3 : 8;
+    const int64_t unit_bytes = (int64_t)sizeof(double) * 3 * (nmd + na) * (paired ? 2 : 1);
+    int64_t C = ((64ll << 20) / unit_bytes) / 128 * 128;
+    if (const char *env = getenv("TCYM_HOST_STEP_CHUNK")) {
+        const long long v = atoll(env);
+        if (v > 0) C = (v + 127) / 128 * 128;
+    }
+    return C < 128 ? 128 : C;
+}
+static bool pinned_host(const void *p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeHost;
+}
+
+// One leapfrog step of a state held in host memory (reference AoS FP64 arrays
+// as tcym_lattice_upload / _download take them), the two transfer directions
+// overlapped with each other and with the step.  The lattice holds the new
+// state afterwards, exactly as after upload + tcym_leapfrog(lat, dt, 1) +
+// download; when a reunitarisation falls due after this step (it must precede
+// the download) those three calls run instead.  With pinned host arrays the
+// pipeline (about a hundred copies, conversions and step chunks tied by
+// events) is captured once as a graph per ping-pong parity and replayed while
+// the arrays, dt and the chunk size stay the same: one launch per step instead
+// of host-issued operations whose issue order would tie the two directions.
+extern "C" int tcym_leapfrog_host(tcym_lattice lat, double dt, const double *U_in, const double *E_in,
+                                  double *U_out, double *E_out) {
+    if (!lat || !U_in || !E_in || !U_out || !E_out) return TCYM_ERR_ARG;
+    tcym_ctx ctx = lat->ctx;
+    cudaSetDevice(ctx->device);
+    if (lat->reunit_period > 0 && lat->steps_since_reunit + 1 >= lat->reunit_period) {
+        int r = tcym_lattice_upload(lat, U_in, E_in);
+        if (!r) r = tcym_leapfrog(lat, dt, 1);
+        if (!r) r = tcym_lattice_download(lat, U_out, E_out);
+        return r;
+    }
+    int r = ensure_staging(lat);
+    if (r) return r;
+    for (auto &st : lat->hs)
+        if (!st) CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    for (auto &ev : lat->hev)
+        if (!ev) CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    bool paired = false;
+    DISPATCH(lat->fmt, paired = L::paired_step(lat->g));
+    const int64_t C = host_step_chunk(lat, paired);
+    const StepCoef<double> c = tcym_coef(lat->a, MODE_LEAPFROG, dt, 0, 0, 0, 0);
+    const void *io[4] = {U_in, E_in, U_out, E_out};
+    const bool graph = pinned_host(U_in) && pinned_host(E_in) && pinned_host(U_out) && pinned_host(E_out);
+    if (!graph) {
+        DISPATCH(lat->fmt, CK(host_step_pipeline<L::FMT_ID>(lat, c, C, U_in, E_in, U_out, E_out)));
+    } else {
+        auto &h = lat->host_graph[lat->cur];
+        if (!h.exec || h.dt != dt || h.chunk != C || h.staging != lat->staging ||
+            memcmp(h.io, io, sizeof io) != 0) {
+            if (h.exec) cudaGraphExecDestroy(h.exec);
+            h = tcym_lattice_s::HostStepGraph{};
+            cudaGraph_t gr = nullptr;
+            CK(cudaStreamBeginCapture(lat->stream, cudaStreamCaptureModeThreadLocal));
+            cudaError_t e = cudaSuccess;
+            DISPATCH(lat->fmt, e = host_step_pipeline<L::FMT_ID>(lat, c, C, U_in, E_in, U_out, E_out));
+            const cudaError_t e2 = cudaStreamEndCapture(lat->stream, &gr);
+            if (e == cudaSuccess) e = e2;
+            if (e == cudaSuccess) e = cudaGraphInstantiate(&h.exec, gr, 0);
+            if (gr) cudaGraphDestroy(gr);
+            if (e != cudaSuccess) {
+                h = tcym_lattice_s::HostStepGraph{};
+                return cuda_fail(ctx, e, "tcym_leapfrog_host: capture of the pipeline");
+            }
+            memcpy(h.io, io, sizeof io);
+            h.dt = dt;
+            h.chunk = C;
+            h.staging = lat->staging;
+        }
+        CK(cudaGraphLaunch(h.exec, lat->stream));
+    }
+    lat->cur ^= 1;
+    ++lat->steps_done;
+    if ((r = maybe_reunitarize(lat))) return r;
+    if ((r = maybe_track(lat, dt, lat->steps_done))) return r;
+    CK(cudaStreamSynchronize(lat->stream));
+    return TCYM_OK;
 }
 
 extern "C" int tcym_langevin(tcym_lattice lat, double dt, double gamma, double T, uint64_t seed, uint64_t step0,

@@ -96,7 +96,7 @@ template <int FMT> static void fill_group(tcym_ensemble ens, FmtGroup &G, int sm
         m.cur = L->cur;
         m.block_begin = blk;
         m.paired = Fmt<FMT>::PAIRED && L->g.nz % 2 == 0;
-        m.tile = m.paired ? tcym_lattice_tile_of(L) : Tile{0, 0, 0, 0, 0};
+        m.tile = m.paired ? tcym_lattice_tile_of(L) : Tile{0, 0, 0, 0, 0, 0};
         if (!m.paired || m.tile.tx != 0) G.general = true;
         blk += m.paired ? (int)tile_blocks(L->g, m.tile) : grid_for(L->g.V, TPB);
         m.red_begin = red;

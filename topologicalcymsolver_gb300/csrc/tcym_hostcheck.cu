@@ -9,6 +9,7 @@
 #include <cstring>
 #include <vector>
 
+#include "tcym_pipeline.h"
 #include "tcym_site.cuh"
 
 using namespace tcym;
@@ -236,6 +237,16 @@ int hc_geodesic(int fmt, const int *n, const void *Uold, const void *Unew, doubl
 int hc_iexp(int fmt, double c, const double *alpha, double *out) {
     HC_DISPATCH(fmt, HH::iexp_aos(c, alpha, out));
     return 0;
+}
+// the issue order of the host-resident step's pipeline: kinds[i] (0 upload,
+// 1 step) of chunks[i]; returns the number of operations (at most cap written)
+int64_t hc_pipeline_schedule(int64_t N, int64_t P, int64_t C, int *kinds, int64_t *chunks, int64_t cap) {
+    int64_t n = 0;
+    pipeline_schedule(N, P, C, [&](int op, int64_t j) {
+        if (n < cap) { kinds[n] = op; chunks[n] = j; }
+        ++n;
+    });
+    return n;
 }
 double hc_normal(uint64_t seed, uint32_t stream, uint64_t step, uint32_t site, uint32_t mu, uint32_t a, int single) {
     double z0, z1;

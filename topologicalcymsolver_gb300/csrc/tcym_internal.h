@@ -44,6 +44,20 @@ struct tcym_lattice_s {
     bool tile_chosen = false;
     cudaStream_t side[2] = {nullptr, nullptr};  // pipelined host transfers (created with the staging)
     cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+    // tcym_leapfrog_host's pipeline: streams for the host-to-device copies, their
+    // conversion, the conversion for the download and the device-to-host copies,
+    // and the events tying them (created on first use)
+    cudaStream_t hs[4] = {nullptr, nullptr, nullptr, nullptr};
+    cudaEvent_t hev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    // tcym_leapfrog_host's pipeline captured as a graph, one per ping-pong parity,
+    // with what it was captured for (host arrays, dt, chunk, staging)
+    struct HostStepGraph {
+        cudaGraphExec_t exec = nullptr;
+        const void *io[4] = {nullptr, nullptr, nullptr, nullptr};
+        double dt = 0;
+        int64_t chunk = 0;
+        const void *staging = nullptr;
+    } host_graph[2];
 };
 
 void tcym_set_error(tcym_ctx ctx, const char *fmt, ...);

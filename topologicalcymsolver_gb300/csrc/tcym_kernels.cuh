@@ -78,11 +78,12 @@ template <class T> StepCoef<T> coef_cast(const StepCoef<double> &c) {
 }
 
 // ------------------------------------------------------------------ kernels
+// sites [s0, s1)
 template <int FMT, bool DO_E, bool DO_U>
 __global__ void __launch_bounds__(threads_for<FMT>(), min_blocks_for<FMT>()) k_step(Geom g, const void *Uin, void *Uout, void *E,
-                                                             StepCoef<typename Fmt<FMT>::T> c) {
-    int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= g.V) return;
+                                                             StepCoef<typename Fmt<FMT>::T> c, int64_t s0, int64_t s1) {
+    const int64_t s = s0 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= s1) return;
     site_step<Fmt<FMT>, DO_E, DO_U>(g, Uin, Uout, E, c, s);
 }
 
@@ -98,7 +99,7 @@ __global__ void __launch_bounds__(kThreadsPair, pair_min_blocks_for<FMT>())
     if constexpr (TILED) {
         if (!tile_pair(g, t, blockIdx.x, threadIdx.x, p, seam)) return;
     } else {
-        const int64_t p0 = (int64_t)blockIdx.x * kThreadsPair;
+        const int64_t p0 = ((int64_t)blockIdx.x + t.b0) * kThreadsPair;
         p = p0 + threadIdx.x;
         if (p >= (g.V >> 1)) return;
         seam = pairs_touch_seam(g, p0, kThreadsPair);
@@ -284,11 +285,12 @@ __global__ void __launch_bounds__(kAosThreads)
 template <int FMT> struct Launch {
     using F = Fmt<FMT>;
     using T = typename F::T;
+    static constexpr int FMT_ID = FMT;
     static constexpr int TPB = threads_for<FMT>();
 
     // t: the block tiling of the paired step (FP32 formats with even nz)
     static cudaError_t step(const Geom &g, const void *Uin, void *Uout, void *E, const StepCoef<double> &cd, bool doE,
-                            bool doU, cudaStream_t st, const Tile &t = Tile{0, 0, 0, 0, 0}) {
+                            bool doU, cudaStream_t st, const Tile &t = Tile{0, 0, 0, 0, 0, 0}) {
         StepCoef<T> c = coef_cast<T>(cd);
         if constexpr (F::PAIRED) {
             if (doE && doU && g.nz % 2 == 0) {
@@ -299,9 +301,29 @@ template <int FMT> struct Launch {
             }
         }
         int grid = grid_for(g.V, TPB);
-        if (doE && doU) k_step<FMT, true, true><<<grid, TPB, 0, st>>>(g, Uin, Uout, E, c);
-        else if (doE) k_step<FMT, true, false><<<grid, TPB, 0, st>>>(g, Uin, Uout, E, c);
-        else k_step<FMT, false, true><<<grid, TPB, 0, st>>>(g, Uin, Uout, E, c);
+        if (doE && doU) k_step<FMT, true, true><<<grid, TPB, 0, st>>>(g, Uin, Uout, E, c, 0, g.V);
+        else if (doE) k_step<FMT, true, false><<<grid, TPB, 0, st>>>(g, Uin, Uout, E, c, 0, g.V);
+        else k_step<FMT, false, true><<<grid, TPB, 0, st>>>(g, Uin, Uout, E, c, 0, g.V);
+        return cudaGetLastError();
+    }
+    // Does step() take the paired kernel (one thread per site pair)?
+    static bool paired_step(const Geom &g) { return F::PAIRED && g.nz % 2 == 0; }
+    // One fused step (E and links) of the storage indices [i0, i1) only: site
+    // pairs when paired_step(g), else sites; i0 a multiple of 128 for pairs.
+    // The linear block mapping.
+    static cudaError_t step_range(const Geom &g, const void *Uin, void *Uout, void *E, const StepCoef<double> &cd,
+                                  int64_t i0, int64_t i1, cudaStream_t st) {
+        StepCoef<T> c = coef_cast<T>(cd);
+        if (i1 <= i0) return cudaSuccess;
+        if constexpr (F::PAIRED) {
+            if (paired_step(g)) {
+                Tile t{0, 0, 0, 0, 0, (int)(i0 / kThreadsPair)};
+                const unsigned blocks = (unsigned)((i1 - i0 + kThreadsPair - 1) / kThreadsPair);
+                k_step_pair<FMT, false><<<blocks, kThreadsPair, 0, st>>>(g, Uin, Uout, E, c, t);
+                return cudaGetLastError();
+            }
+        }
+        k_step<FMT, true, true><<<grid_for(i1 - i0, TPB), TPB, 0, st>>>(g, Uin, Uout, E, c, i0, i1);
         return cudaGetLastError();
     }
     static cudaError_t flow_cb(const Geom &g, void *U, int parity, int mu, const double *fc, const double *cn,

@@ -205,14 +205,15 @@ TCYM_HD bool pairs_touch_seam(const Geom &g, int64_t p0, int64_t n) {
 struct Tile {
     int tx, ty, lx;          // tile extents; lx = log2(tx)
     int tiles_x, tiles_y;    // tiles per z-plane
+    int b0;                  // linear mapping: the launch starts at pair 128 b0 (a range of pairs)
 };
 // tx = 0: linear; else a tx x (128 / tx) tile, tx a power of two from 1 to 128
 TCYM_HD Tile make_tile(const Geom &g, int tx) {
-    if (tx <= 0) return Tile{0, 0, 0, 0, 0};
+    if (tx <= 0) return Tile{0, 0, 0, 0, 0, 0};
     int lx = 0;
     while ((1 << lx) < tx) ++lx;
     const int ty = 128 / tx;
-    return Tile{tx, ty, lx, (g.nx + tx - 1) / tx, (g.ny + ty - 1) / ty};
+    return Tile{tx, ty, lx, (g.nx + tx - 1) / tx, (g.ny + ty - 1) / ty, 0};
 }
 TCYM_HD int64_t tile_blocks(const Geom &g, const Tile &t) {
     const int64_t Vh = g.V >> 1;
@@ -223,8 +224,8 @@ TCYM_HD int64_t tile_blocks(const Geom &g, const Tile &t) {
 // false: the thread has no pair (a partial tile or the last linear block).
 TCYM_HD bool tile_pair(const Geom &g, const Tile &t, int64_t b, int tid, int64_t &p, bool &seam) {
     if (t.tx == 0) {
-        p = b * 128 + tid;
-        seam = pairs_touch_seam(g, b * 128, 128);
+        p = (b + t.b0) * 128 + tid;
+        seam = pairs_touch_seam(g, (b + t.b0) * 128, 128);
         return p < (g.V >> 1);
     }
     const int64_t per_plane = (int64_t)t.tiles_x * t.tiles_y;
