@@ -119,6 +119,12 @@ int tcym_lattice_download(tcym_lattice lat, double *U_aos, double *E_aos);
  * Host buffers in pinned memory (cudaMallocHost / cudaHostRegister) make the copies asynchronous. */
 int tcym_leapfrog_host(tcym_lattice lat, double dt, const double *U_in, const double *E_in, double *U_out,
                        double *E_out);
+/* Block(GaugeLinks**) + Block(ElectricFields**) (LATTICE/GaugeLinks.cpp:124-145,
+ * LATTICE/ElectricFields.cpp:113-127) into dst, a lattice of the same group and
+ * precision with half the (even) extents of src: dst's links become
+ * U'_mu(x) = U_mu(2x) U_mu(2x + mu) (products in FP64), its fields zero and its
+ * spacings twice src's. */
+int tcym_lattice_block(const tcym_lattice src, tcym_lattice dst);
 /* dst <- src (same group and extents; any precisions): Copy() of GaugeLinks.cpp:91-107
  * and ElectricFields.cpp:90-104. */
 int tcym_lattice_copy(tcym_lattice dst, const tcym_lattice src);
@@ -157,14 +163,21 @@ int tcym_lattice_tile(tcym_lattice lat, int *tx, int *ty);
 int tcym_lattice_set_tile(tcym_lattice lat, int tx, int ty);
 
 /* ---------------------------------------------------- cooled Chern-Simons number
- * ChernSimonsNumber::CoolingMethod (TOPOLOGY/CoolingMethod.cpp) at blocking level 0,
- * the level of its real-time measurement (SphaleronSimulation.cpp:230-236).  The
- * object holds the last two cooled copies UOld, UNew of the lattice's links; a copy
- * is made as Cooling::CoolNSave does (GRADIENTFLOW/Cooling.cpp:156-175): max_steps
- * GradientFlow::StandardUpdate steps of dtau = sqrt_dctau^2 from E = 0 (the
- * reference: 128 steps, SphaleronSimulation.cpp:230).  The lattice is only read. */
+ * ChernSimonsNumber::CoolingMethod (TOPOLOGY/CoolingMethod.cpp).  The object holds
+ * the last two cooled copies UOld, UNew of the lattice's links; a copy is made as
+ * Cooling::CoolNSave does (GRADIENTFLOW/Cooling.cpp:69-175): max_steps
+ * GradientFlow::StandardUpdate steps of DcTau = sqrt_dctau^2 (a_x a_y a_z)^(2/3) from
+ * E = 0 (the reference: 128 steps, SphaleronSimulation.cpp:230).  With a blocking
+ * level L > 0 (StandardBlockingLevel) links and fields are blocked (tcym_lattice_block)
+ * after steps block_frequency * 8^b, b < L (Cooling::BlockFrequency), so the cooled
+ * copies have the extents divided by 2^L: the extents must be divisible by 2^L and
+ * block_frequency * 8^(L-1) <= max_steps.  tcym_cooling_create is level 0, the level of
+ * the reference's real-time measurement (SphaleronSimulation.cpp:230-236).  The lattice
+ * is only read. */
 typedef struct tcym_cooling_s *tcym_cooling;
 int tcym_cooling_create(tcym_lattice lat, int max_steps, double sqrt_dctau, tcym_cooling *out);
+int tcym_cooling_create_ex(tcym_lattice lat, int max_steps, double sqrt_dctau, int blocking_level,
+                           int block_frequency, tcym_cooling *out);
 int tcym_cooling_destroy(tcym_cooling c);
 /* CoolingMethod::Start (:124-135): UNew = the cooled links, UOld = UNew. */
 int tcym_cooling_start(tcym_cooling c);
@@ -179,6 +192,9 @@ int tcym_cooling_update(tcym_cooling c, int measure, double *delta);
 int tcym_cooling_delta_ncs(tcym_cooling c, int norder, double *out);
 /* the sum of the measured updates (ChernSimonsNumber::DeltaNCsCoolRealTime) */
 int tcym_cooling_total(tcym_cooling c, double *out);
+/* the latest cooled links (CoolingMethod::UOld, blocked to the extents divided by
+ * 2^level) in the reference's AoS layout; TCYM_ERR_STATE before tcym_cooling_start. */
+int tcym_cooling_links(tcym_cooling c, double *U_aos);
 
 /* ------------------------------------------------------- configuration files
  * The reference's text format (IO/SaveConfiguration.cpp:3-56, IO/LoadConfiguration.cpp:3-120):
@@ -240,7 +256,8 @@ int tcym_update_u(tcym_lattice lat, double dt);
 int tcym_langevin(tcym_lattice lat, double dt, double gamma, double T, uint64_t seed, uint64_t step0, int nsteps);
 /* GradientFlow::StandardUpdate (calibrate = 0) / CalibrationUpdate (calibrate =
  * TCYM_NCS_IMPROVED or TCYM_NCS_CLOVER) (GRADIENTFLOW/GradientFlow.cpp:150-188), nsteps
- * flow steps of size dtau (the reference's DcTau = SqrtDcTauOverSpacing^2), all links at
+ * flow steps of size dtau (the reference's DcTau = SqrtDcTauOverSpacing^2 (a_x a_y a_z)^(2/3),
+ * GradientFlow.cpp:150; calibration: unit spacings), all links at
  * once or checkerboarded.  With calibrate, *dncs receives sum dtau/2 [NCsDot(U,F) +
  * NCsDot(U',F)] with the chosen E.B operator (the reference uses the improved one).
  * In checkerboard mode F is the force of the state before each sweep.  The field array

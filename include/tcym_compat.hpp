@@ -463,37 +463,80 @@ inline void CalibrationUpdate(GaugeLinks *U, ElectricFields *E) {
 }
 }  // namespace GradientFlow
 
+// Block(GaugeLinks**) (LATTICE/GaugeLinks.cpp:124-145): the links replaced by the
+// blocked ones, U'_mu(x) = U_mu(2x) U_mu(2x + mu), on half the extents and twice
+// the spacings (computed on the device, tcym_lattice_block)
+inline void Block(GaugeLinks **UOld) {
+    GaugeLinks *u = *UOld;
+    GaugeLinks *n = new GaugeLinks(u->N[0] / 2, u->N[1] / 2, u->N[2] / 2, (INT)(2 * u->a[0]), (INT)(2 * u->a[1]),
+                                   (INT)(2 * u->a[2]));
+    tcym_lattice src = tcym_compat::bind(u, nullptr);
+    tcym_compat::check(tcym_lattice_block(src, tcym_compat::bind(n, nullptr)), "block links");
+    n->fresh = tcym_compat::Fresh::Device;
+    delete u;
+    *UOld = n;
+}
+// Block(ElectricFields**) (LATTICE/ElectricFields.cpp:113-127): zero fields on half the extents
+inline void Block(ElectricFields **EOld) {
+    ElectricFields *e = *EOld;
+    ElectricFields *n = new ElectricFields(e->N[0] / 2, e->N[1] / 2, e->N[2] / 2, (INT)(2 * e->a[0]),
+                                           (INT)(2 * e->a[1]), (INT)(2 * e->a[2]));
+    n->SetZero();
+    delete e;
+    *EOld = n;
+}
+
 namespace Cooling {
-// CoolNSave (GRADIENTFLOW/Cooling.cpp:156-179): flow a copy of UHot with E = 0 for
-// MaxCoolingSteps steps and store the result in UCold (blocking is not supported).
+inline INT BlockFrequency = 0;
+// CoolNSave (GRADIENTFLOW/Cooling.cpp:156-179) with Perform's blocking (:69-143):
+// flow a copy of UHot from E = 0 for MaxCoolingSteps steps, blocking links and
+// fields after each step that is a multiple of BlockFrequency 8^b while fewer than
+// MaxBlockingNumber Blocks were made; the result goes to UCold (of the blocked size).
 inline void CoolNSave(std::string, DOUBLE MaxCoolingSteps, INT MaxBlockingNumber, GaugeLinks *UHot, GaugeLinks *UCold) {
-    if (MaxBlockingNumber != 0) throw std::invalid_argument("tcym: lattice blocking during cooling is not supported");
-    GaugeLinks U(UHot->N[0], UHot->N[1], UHot->N[2], (INT)UHot->a[0], (INT)UHot->a[1], (INT)UHot->a[2]);
-    ElectricFields E(UHot->N[0], UHot->N[1], UHot->N[2], (INT)UHot->a[0], (INT)UHot->a[1], (INT)UHot->a[2]);
-    Copy(&U, UHot);
-    E.SetZero();
+    GaugeLinks *U = new GaugeLinks(UHot->N[0], UHot->N[1], UHot->N[2], (INT)UHot->a[0], (INT)UHot->a[1], (INT)UHot->a[2]);
+    ElectricFields *E =
+        new ElectricFields(UHot->N[0], UHot->N[1], UHot->N[2], (INT)UHot->a[0], (INT)UHot->a[1], (INT)UHot->a[2]);
+    Copy(U, UHot);
+    E->SetZero();
     GradientFlow::Reset();
-    while (GradientFlow::CoolingSteps < MaxCoolingSteps) GradientFlow::StandardUpdate(&U, &E);
-    Copy(UCold, &U);
+    INT blocking = 0;
+    while (GradientFlow::CoolingSteps < MaxCoolingSteps) {
+        GradientFlow::StandardUpdate(U, E);
+        if (blocking < MaxBlockingNumber && BlockFrequency > 0 &&
+            GradientFlow::CoolingSteps % (BlockFrequency * (INT)std::pow(8, blocking)) == 0) {
+            ::Block(&U);
+            ::Block(&E);
+            ++blocking;
+        }
+    }
+    if (UCold->Volume != U->Volume) {
+        delete U;
+        delete E;
+        throw std::invalid_argument("tcym: CoolNSave: UCold does not have the blocked extents");
+    }
+    Copy(UCold, U);
+    delete U;
+    delete E;
 }
 }  // namespace Cooling
 
 namespace ChernSimonsNumber {
 inline DOUBLE DeltaNCsCoolRealTime = 0.0;
-// CoolingMethod (TOPOLOGY/CoolingMethod.cpp) on GLinks::U at blocking level 0, its
-// real-time measurement level (SphaleronSimulation.cpp:236); the cooled copies live
-// on the device (tcym_cooling_*), flowed with GradientFlow::SqrtDcTauOverSpacing.
+// CoolingMethod (TOPOLOGY/CoolingMethod.cpp) on GLinks::U at StandardBlockingLevel
+// (the reference's drivers use 0, SphaleronSimulation.cpp:236) with Cooling::BlockFrequency;
+// the cooled copies live on the device (tcym_cooling_*), flowed with
+// GradientFlow::SqrtDcTauOverSpacing.
 namespace CoolingMethod {
 inline INT StandardBlockingLevel = 0;
 inline INT StandardCoolingMaxSteps = 128;
 inline tcym_cooling state = nullptr;
 // Init (:19-32)
 inline void Init() {
-    if (StandardBlockingLevel != 0)
-        throw std::invalid_argument("tcym: cooled N_CS with lattice blocking is not supported");
     if (state) tcym_cooling_destroy(state);
-    tcym_compat::check(tcym_cooling_create(tcym_compat::bind(GLinks::U, EFields::E), (int)StandardCoolingMaxSteps,
-                                           GradientFlow::SqrtDcTauOverSpacing, &state),
+    state = nullptr;
+    tcym_compat::check(tcym_cooling_create_ex(tcym_compat::bind(GLinks::U, EFields::E), (int)StandardCoolingMaxSteps,
+                                              GradientFlow::SqrtDcTauOverSpacing, (int)StandardBlockingLevel,
+                                              (int)Cooling::BlockFrequency, &state),
                        "cooling init");
 }
 // Start (:124-135)

@@ -89,6 +89,9 @@ class Port:
         f("thermalize").restype = ctypes.c_int
         f("ilog").argtypes = [ctypes.c_double, _dbl_p, _dbl_p]
         f("cool").argtypes = [_int_p, _dbl_p, ctypes.c_double, ctypes.c_int]
+        f("block").argtypes = [_int_p, _dbl_p, _dbl_p]
+        f("cool_blocked").argtypes = [_int_p, _dbl_p, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                      _dbl_p]
         f("geodesic").argtypes = [_int_p, _dbl_p, _dbl_p, ctypes.c_double, _dbl_p, _dbl_p]
         f("cooled_delta_ncs").argtypes = [_int_p, _dbl_p, _dbl_p, ctypes.c_int]
         f("cooled_delta_ncs").restype = ctypes.c_double
@@ -161,6 +164,18 @@ class Port:
 
     def cool(self, shape, U, sqrt_dctau, nsteps):
         self._f("cool")(_n(shape), _p(U), sqrt_dctau, nsteps)
+
+    def block(self, shape, U):
+        """Block(GaugeLinks**): the links of the lattice of half the extents."""
+        Ub, _ = empty_fields(self.nc, tuple(k // 2 for k in shape))
+        self._f("block")(_n(shape), _p(U), _p(Ub))
+        return Ub
+
+    def cool_blocked(self, shape, U, sqrt_dctau, nsteps, level, block_frequency):
+        """Cooling::CoolNSave with `level` Blocks: the cooled links on shape / 2^level."""
+        Uc, _ = empty_fields(self.nc, tuple(k >> level for k in shape))
+        self._f("cool_blocked")(_n(shape), _p(U), sqrt_dctau, nsteps, level, block_frequency, _p(Uc))
+        return Uc
 
     def geodesic(self, shape, Uold, Unew, c):
         Um, Em = empty_fields(self.nc, shape)
@@ -300,8 +315,9 @@ class Ref:
     def cooling_update(self, measure):
         return self.lib.ref_cooling_update(measure)
 
-    def cooling_links(self):
-        U, _ = empty_fields(self.nc, self.shape)
+    def cooling_links(self, blocking=0):
+        """UOld of CoolingMethod (on the extents divided by 2^blocking)."""
+        U, _ = empty_fields(self.nc, tuple(k >> blocking for k in self.shape))
         self.lib.ref_cooling_links(_p(U))
         return U
 

@@ -47,5 +47,19 @@ int main(int argc, char **argv) {
     GradientFlow::Reset();
     for (int s = 0; s < 3; ++s) GradientFlow::CalibrationUpdate(GLinks::U, EFields::E);
     std::printf("calibration %.17g %.17g\n", ChernSimonsNumber::DeltaNCsCooling, GradientFlow::CoolingTime());
+    // blocked cooling: one Block (after 2 of 6 steps) onto L/2 extents, spacing 2
+    Cooling::BlockFrequency = 2;
+    GaugeLinks UBlocked(L / 2, L / 2, L / 2, 2, 2, 2);
+    Cooling::CoolNSave("coolb", 6, 1, GLinks::U, &UBlocked);
+    std::printf("cooled_blocked %.17g %.17g\n", (double)std::real(*UBlocked.Get(0, 0, 0, 0)),
+                (double)std::real(*UBlocked.Get(1, 2, 2, 2)));
+    // cooled real-time N_CS at StandardBlockingLevel 1
+    ChernSimonsNumber::CoolingMethod::StandardBlockingLevel = 1;
+    ChernSimonsNumber::CoolingMethod::StandardCoolingMaxSteps = 6;
+    ChernSimonsNumber::CoolingMethod::Init();
+    ChernSimonsNumber::CoolingMethod::Start();
+    for (int s = 0; s < 10; ++s) Dynamics::Update();
+    ChernSimonsNumber::CoolingMethod::Update(1);
+    std::printf("cooled_ncs %.17g\n", ChernSimonsNumber::DeltaNCsCoolRealTime);
     return 0;
 }

@@ -168,6 +168,33 @@ def cooling():
                         cooled=np.array(cooled), steps=16, sqrt_dctau=np.sqrt(0.02), dt=0.05, every=20)
 
 
+def cooling_blocked():
+    """CoolingMethod with lattice blocking (StandardBlockingLevel 1 and 2) on SU(2) 8^3:
+    the cooled ΔN_CS totals and cooled (blocked) links of three updates."""
+    P, R = oracle.Port(2), oracle.Ref(2)
+    shape = (8, 8, 8)
+    U, E = oracle.empty_fields(2, shape)
+    P.random_links(shape, U, 0.5, 5)
+    P.gaussian_efield(shape, E, 0.7, 6)
+    P.gauss_restore(shape, U, E, 1e-14, 10000)
+    out = {"U0": U, "E0": E, "dt": 0.05, "every": 20, "sqrt_dctau": np.sqrt(0.02)}
+    for level, steps, bf in ((1, 16, 2), (2, 12, 1)):
+        R.init(shape)
+        R.set(U, E)
+        R.cooling_init(level, steps, bf, np.sqrt(0.02))
+        R.cooling_start()
+        totals, cooled = [], []
+        for _ in range(3):
+            R.leapfrog(0.05, 20)
+            totals.append(R.cooling_update(1))
+            cooled.append(R.cooling_links(level))
+        out[f"totals{level}"] = np.array(totals)
+        out[f"cooled{level}"] = np.array(cooled)
+        out[f"steps{level}"] = steps
+        out[f"bf{level}"] = bf
+    np.savez_compressed(os.path.join(HERE, "ref_cooling_blocked_su2.npz"), **out)
+
+
 if __name__ == "__main__":
     oracle.build()
     if not (oracle.ref_available(2) and oracle.ref_available(3)):
@@ -179,6 +206,7 @@ if __name__ == "__main__":
     for nc in (2, 3):
         thermalize(nc)
     cooling()
+    cooling_blocked()
     for nc in (2, 3):
         configuration(nc)
     for f in sorted(os.listdir(HERE)):

@@ -2,7 +2,7 @@
 
 tests/compat/driver.cpp is written against the reference's API (Lattice::Init,
 InitialConditions::SetZero, ThermalDynamics::ReassignElectricFields,
-Dynamics::Update, Observables::Bulk, LangevinDynamics::Update, Cooling::CoolNSave,
+Dynamics::Update, Observables::Bulk, LangevinDynamics::Update, Cooling::CoolNSave (also with a Block),
 GradientFlow::CalibrationUpdate, the E.B operators).  It is compiled with g++
 against libtcym.so for SU(2) and SU(3), run on the GPU, and every number it
 prints is compared with the FP64 oracle running the same sequence.
@@ -71,3 +71,15 @@ def test_reference_style_driver_matches_oracle(oracle_port, nc, tmp_path):
     assert close(got["cooled"][0][0], Uc[0, 0, 0])
     dn = P.flow(shape, U, E, dtau, 3, 1)
     assert close(got["calibration"][0][0], dn) and close(got["calibration"][0][1], 3 * dtau)
+    # Cooling::CoolNSave with one Block, then CoolingMethod at StandardBlockingLevel 1
+    s = 0.1414213562373095
+    half = L // 2
+    sb = lambda x, y, z: x + half * (y + half * z)  # noqa: E731
+    Ub = P.cool_blocked(shape, U, s, 6, 1, 2)
+    assert close(got["cooled_blocked"][0][0], Ub[sb(0, 0, 0), 0, 0])
+    assert close(got["cooled_blocked"][0][1], Ub[sb(1, 2, 2), 2, 0])
+    old = Ub
+    P.leapfrog(shape, U, E, 0.05, 10)
+    new = P.cool_blocked(shape, U, s, 6, 1, 2)
+    d = P.cooled_delta_ncs((half, half, half), old, new, 1)
+    assert abs(got["cooled_ncs"][0][0] - d) <= TOL * max(abs(d), 1e-3), (got["cooled_ncs"], d)

@@ -160,3 +160,65 @@ def test_cooled_delta_ncs_equals_reference(oracle_port):
         assert abs(total - d["totals"][k]) < 1e-12, (k, total, d["totals"][k])
         assert rel(new, d["cooled"][k]) < 1e-12
         old = new
+
+
+@pytest.mark.parametrize("level", [1, 2])
+def test_blocked_cooling_equals_reference(oracle_port, level):
+    """CoolingMethod with StandardBlockingLevel 1 and 2 (Cooling::Perform's Blocks after
+    steps BlockFrequency 8^b, each doubling the spacing): the oracle's blocked cooling
+    reproduces the reference's cooled links on the blocked extents and its ΔN_CS."""
+    d = load("ref_cooling_blocked_su2.npz")
+    P = oracle_port[2]
+    shape = (8, 8, 8)
+    small = tuple(k >> level for k in shape)
+    U, E = d["U0"].copy(), d["E0"].copy()
+    steps, bf, s = int(d[f"steps{level}"]), int(d[f"bf{level}"]), float(d["sqrt_dctau"])
+    old = P.cool_blocked(shape, U, s, steps, level, bf)
+    total = 0.0
+    for k in range(3):
+        P.leapfrog(shape, U, E, float(d["dt"]), int(d["every"]))
+        new = P.cool_blocked(shape, U, s, steps, level, bf)
+        total += P.cooled_delta_ncs(small, old, new, 1)
+        assert rel(new, d[f"cooled{level}"][k]) < 1e-12
+        assert abs(total - d[f"totals{level}"][k]) < 1e-12, (k, total, d[f"totals{level}"][k])
+        old = new
+
+
+@pytest.mark.parametrize("nc", [2, 3])
+def test_blocked_cooling_composes_flow_and_block(oracle_port, nc):
+    """The oracle's blocked cooling equals its own pieces: bf flow steps, Block, the
+    remaining steps at the same dtau (the spacing factors cancel), for both groups."""
+    P = oracle_port[nc]
+    shape = (4, 4, 6)
+    U, E = oracle.empty_fields(nc, shape)
+    P.random_links(shape, U, 0.5, 9)
+    s, steps, bf = 0.15, 7, 3
+    got = P.cool_blocked(shape, U, s, steps, 1, bf)
+    W, F = U.copy(), np.zeros_like(E)
+    P.flow(shape, W, F, s * s, bf, 0)
+    Wb = P.block(shape, W)
+    small = (2, 2, 3)
+    _, Fb = oracle.empty_fields(nc, small)
+    P.flow(small, Wb, Fb, s * s, steps - bf, 0)
+    assert np.abs(got - Wb).max() < 1e-13
+
+
+def test_block_is_the_product_of_two_links(oracle_port):
+    """Block(GaugeLinks**) on SU(3): U'_mu(x) = U_mu(2x) U_mu(2x + mu), checked link by link."""
+    P = oracle_port[3]
+    shape = (4, 6, 2)
+    U, _ = oracle.empty_fields(3, shape)
+    P.random_links(shape, U, 0.6, 7)
+    Ub = P.block(shape, U)
+    nx, ny = shape[0], shape[1]
+
+    def mat(v):
+        return (v[0::2] + 1j * v[1::2]).reshape(3, 3, order="F")  # column-major complex 3x3
+
+    for (x, y, z) in [(0, 0, 0), (1, 2, 0), (1, 1, 0)]:
+        s0 = 2 * x + nx * (2 * y + ny * 2 * z)
+        sb = x + (nx // 2) * (y + (ny // 2) * z)
+        for mu, step in enumerate((1, nx, nx * ny)):
+            s1 = s0 + step if mu < 2 or 2 * z + 1 < shape[2] else s0 + step - nx * ny * shape[2]
+            ref = mat(U[s0, mu]) @ mat(U[s1, mu])
+            assert np.abs(mat(Ub[sb, mu]) - ref).max() < 1e-14

@@ -114,6 +114,10 @@ def library() -> ctypes.CDLL:
         "tcym_lattice_bytes": ([ctypes.c_void_p, ctypes.POINTER(ctypes.c_size_t)], ctypes.c_int),
         "tcym_lattice_upload": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
         "tcym_lattice_download": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+        "tcym_lattice_block": ([ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+        "tcym_cooling_links": ([ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+        "tcym_cooling_create_ex": ([ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int,
+                                    ctypes.c_void_p], ctypes.c_int),
         "tcym_leapfrog_host": ([ctypes.c_void_p, ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                 ctypes.c_void_p], ctypes.c_int),
         "tcym_lattice_copy": ([ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
@@ -270,6 +274,12 @@ class Lattice:
         self.ctx.check(self.lib.tcym_leapfrog_host(self.h, dt, _ptr(U), _ptr(E), _ptr(U_out), _ptr(E_out)))
         return U_out, E_out
 
+    def block_into(self, dst: "Lattice"):
+        """Block(GaugeLinks**) + Block(ElectricFields**): dst (half the even extents, same
+        group and precision) gets U'_mu(x) = U_mu(2x) U_mu(2x + mu), zero fields and
+        twice the spacings."""
+        self.ctx.check(self.lib.tcym_lattice_block(self.h, dst.h))
+
     def copy_from(self, other: "Lattice"):
         self.ctx.check(self.lib.tcym_lattice_copy(self.h, other.h))
 
@@ -413,14 +423,18 @@ def read_configuration(nc: int, shape, ufile=None, efile=None):
 
 
 class Cooling:
-    """ChernSimonsNumber::CoolingMethod at blocking level 0 (tcym_cooling_*): cooled
-    copies of a lattice's links and the cooled real-time Delta N_CS between them."""
+    """ChernSimonsNumber::CoolingMethod (tcym_cooling_*): cooled copies of a lattice's
+    links (blocked blocking_level times, after steps block_frequency 8^b) and the
+    cooled real-time Delta N_CS between them."""
 
-    def __init__(self, lat: "Lattice", max_steps: int = 128, sqrt_dctau: float = 0.125 ** 0.5):
+    def __init__(self, lat: "Lattice", max_steps: int = 128, sqrt_dctau: float = 0.125 ** 0.5,
+                 blocking_level: int = 0, block_frequency: int = 0):
         self.lat, self.ctx, self.lib = lat, lat.ctx, lat.lib
         h = ctypes.c_void_p()
-        self.ctx.check(self.lib.tcym_cooling_create(lat.h, max_steps, sqrt_dctau, ctypes.byref(h)))
+        self.ctx.check(self.lib.tcym_cooling_create_ex(lat.h, max_steps, sqrt_dctau, blocking_level, block_frequency,
+                                                       ctypes.byref(h)))
         self.h = h
+        self.level = blocking_level
 
     def start(self):
         self.ctx.check(self.lib.tcym_cooling_start(self.h))
@@ -434,6 +448,13 @@ class Cooling:
         d = ctypes.c_double()
         self.ctx.check(self.lib.tcym_cooling_delta_ncs(self.h, norder, ctypes.byref(d)))
         return d.value
+
+    def links(self):
+        """The latest cooled links (AoS FP64, on the lattice's extents / 2^blocking_level)."""
+        V = self.lat.V >> (3 * self.level)
+        U = np.empty((V, 3, NM[self.lat.nc]))
+        self.ctx.check(self.lib.tcym_cooling_links(self.h, _ptr(U)))
+        return U
 
     def total(self) -> float:
         d = ctypes.c_double()

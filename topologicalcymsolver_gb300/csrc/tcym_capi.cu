@@ -332,6 +332,29 @@ extern "C" int tcym_lattice_download(tcym_lattice lat, double *U_aos, double *E_
     return TCYM_OK;
 }
 
+// Block(GaugeLinks**) and Block(ElectricFields**) (LATTICE/GaugeLinks.cpp:124-145,
+// LATTICE/ElectricFields.cpp:113-127) into an existing lattice: dst has half the
+// (even) extents of src, the same group and precision; it receives the blocked
+// links U'_mu(x) = U_mu(2x) U_mu(2x + mu), zero fields and twice src's spacings.
+extern "C" int tcym_lattice_block(const tcym_lattice src, tcym_lattice dst) {
+    if (!dst || !src) return TCYM_ERR_ARG;
+    tcym_ctx ctx = dst->ctx;
+    const Geom &gs = src->g, &gd = dst->g;
+    if (dst->fmt != src->fmt || ((gs.nx | gs.ny | gs.nz) & 1) || gd.nx * 2 != gs.nx || gd.ny * 2 != gs.ny ||
+        gd.nz * 2 != gs.nz) {
+        tcym_set_error(ctx, "tcym_lattice_block: dst must have the group and precision of src and half its even extents");
+        return TCYM_ERR_ARG;
+    }
+    cudaSetDevice(ctx->device);
+    CK(cudaStreamSynchronize(src->stream));
+    DISPATCH(dst->fmt, CK(L::block(gs, gd, src->U[src->cur], dst->U[dst->cur], dst->stream)));
+    CK(cudaMemsetAsync(dst->E, 0, 3 * tcym_field_bytes(dst->fmt) * tcym_stored_sites(dst->fmt, gd.V), dst->stream));
+    for (int i = 0; i < 3; ++i) dst->a[i] = 2.0 * src->a[i];
+    drop_host_graphs(dst);  // their step coefficients hold the old spacings
+    CK(cudaStreamSynchronize(dst->stream));
+    return TCYM_OK;
+}
+
 extern "C" int tcym_lattice_copy(tcym_lattice dst, const tcym_lattice src) {
     if (!dst || !src) return TCYM_ERR_ARG;
     tcym_ctx ctx = dst->ctx;

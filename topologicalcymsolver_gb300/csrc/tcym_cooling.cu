@@ -1,19 +1,27 @@
 // Cooled real-time Chern-Simons number: ChernSimonsNumber::CoolingMethod
-// (TOPOLOGY/CoolingMethod.cpp) at blocking level 0, the level its real-time
-// measurement runs at (StandardBlockingLevel, SphaleronSimulation.cpp:236).
+// (TOPOLOGY/CoolingMethod.cpp) at any standard blocking level.
 //
-// The object keeps three lattices of the caller's format and extents: UOld
-// and UNew (the last two cooled configurations, Init :19-32) and a scratch
-// lattice holding UMid/EMid of the geodesic between them.  Cooling
-// (Cooling::CoolNSave, GRADIENTFLOW/Cooling.cpp:156-175) copies the caller's
-// links into UNew, sets its E to zero and runs max_steps simultaneous flow
-// steps of dtau = sqrt_dctau^2 (GradientFlow::StandardUpdate,
-// GradientFlow.cpp:150-165) through tcym_flow.  The geodesic
-// (SUNc/AdvancedOperations.cpp:432-442) runs per link in FP64 (k_geodesic), and
-// NCsDot = improved E.B / (8 pi^2) (ChernSimonsDerivative.cpp:31-49) through
-// tcym_edotb_improved, so every reduction is the library's fixed-order FP64 one.
+// The object keeps UOld and UNew (the last two cooled configurations, Init
+// :19-32), at the caller's extents divided by 2^level, and a scratch lattice
+// of that size holding UMid/EMid of the geodesic between them.  Cooling
+// (Cooling::CoolNSave and Perform, GRADIENTFLOW/Cooling.cpp:69-175) copies the
+// caller's links, sets E to zero and runs max_steps simultaneous flow steps
+// (GradientFlow::StandardUpdate, GradientFlow.cpp:150-165) through tcym_flow;
+// with blocking, the b-th Block of links and fields (Cooling.cpp:123-143)
+// comes after step block_frequency * 8^b, onto a lattice of half the extents
+// and twice the spacings, until the level is reached.  Each flow step has
+// DcTau = sqrt_dctau^2 (a_x a_y a_z)^(2/3) of the lattice it runs on
+// (GradientFlow.cpp:150).  The geodesic (SUNc/AdvancedOperations.cpp:432-442)
+// runs per link in FP64 (k_geodesic), and NCsDot = improved E.B / (8 pi^2)
+// (ChernSimonsDerivative.cpp:31-49) through tcym_edotb_improved, so every
+// reduction is the library's fixed-order FP64 one.  EMid's conversion to
+// field units (cE_mu = a^3 / a_mu^2, CoolingMethod.cpp:39-45) and E.B's
+// weights (cS_mu = a_mu^2 / a^3, ChernSimonsOperators.cpp:91-95) multiply to
+// one, so neither is applied at any spacing.
 #include <cmath>
 #include <new>
+#include <utility>
+#include <vector>
 
 #include "../../include/tcym.h"
 #include "tcym_batch.cuh"
@@ -24,6 +32,11 @@ using namespace tcym;
 struct tcym_cooling_s {
     tcym_lattice hot = nullptr;
     tcym_lattice uold = nullptr, unew = nullptr, mid = nullptr;
+    // blocking: work[b] holds the cooled links at blocking number b < level
+    // (work[0] the caller's extents); the last Block writes into unew
+    static constexpr int kMaxLevel = 8;
+    tcym_lattice work[kMaxLevel] = {};
+    int level = 0, block_frequency = 0;
     int max_steps = 0;
     double sqrt_dctau = 0.0;
     double real_time = 0.0;  // DeltaNCsCoolRealTime
@@ -52,13 +65,30 @@ int copy_links(tcym_lattice dst, tcym_lattice src) {
     return TCYM_OK;
 }
 
-// Cooling::CoolNSave at blocking level 0: UNew = the hot links cooled from E = 0
+// GradientFlow's DcTau on lattice l (GradientFlow.cpp:150, aScale = 1)
+double dctau(tcym_cooling c, tcym_lattice l) {
+    return c->sqrt_dctau * c->sqrt_dctau * std::cbrt(l->a[0] * l->a[1] * l->a[2] * l->a[0] * l->a[1] * l->a[2]);
+}
+
+// Cooling::CoolNSave: UNew = the hot links cooled from E = 0 with level Blocks
+// (Perform, Cooling.cpp:69-143: the b-th after step block_frequency 8^b)
 int cool(tcym_cooling c) {
-    int r = copy_links(c->unew, c->hot);
+    tcym_lattice cur = c->level ? c->work[0] : c->unew;
+    int r = copy_links(cur, c->hot);
     if (r) return r;
-    CKC(c->hot->ctx, cudaMemsetAsync(c->unew->E, 0, field_bytes(c->unew), c->unew->stream));
+    CKC(c->hot->ctx, cudaMemsetAsync(cur->E, 0, field_bytes(cur), cur->stream));
     double unused = 0.0;
-    return tcym_flow(c->unew, c->sqrt_dctau * c->sqrt_dctau, c->max_steps, TCYM_FLOW_SIMULTANEOUS, 0, &unused);
+    int steps = 0;
+    for (int b = 0;; ++b) {
+        // flow up to the next Block, or to the end
+        const int upto = b < c->level ? c->block_frequency << (3 * b) : c->max_steps;
+        if ((r = tcym_flow(cur, dctau(c, cur), upto - steps, TCYM_FLOW_SIMULTANEOUS, 0, &unused))) return r;
+        steps = upto;
+        if (b == c->level) return TCYM_OK;
+        tcym_lattice next = b + 1 < c->level ? c->work[b + 1] : c->unew;
+        if ((r = tcym_lattice_block(cur, next))) return r;
+        cur = next;
+    }
 }
 
 int ncs_dot(tcym_lattice l, double *out) {
@@ -113,17 +143,38 @@ int delta_ncs(tcym_cooling c, int norder, double *out) {
 
 }  // namespace
 
-extern "C" int tcym_cooling_create(tcym_lattice lat, int max_steps, double sqrt_dctau, tcym_cooling *out) {
-    if (!lat || !out || max_steps < 0 || !(sqrt_dctau >= 0)) return TCYM_ERR_ARG;
+extern "C" int tcym_cooling_create_ex(tcym_lattice lat, int max_steps, double sqrt_dctau, int blocking_level,
+                                      int block_frequency, tcym_cooling *out) {
+    if (!lat || !out || max_steps < 0 || !(sqrt_dctau >= 0) || blocking_level < 0 ||
+        blocking_level >= tcym_cooling_s::kMaxLevel)
+        return TCYM_ERR_ARG;
     *out = nullptr;
+    if (blocking_level > 0) {
+        // every Block must fall within the cooling steps, on extents divisible by 2^level
+        const int f = 1 << blocking_level;
+        const long long last = block_frequency > 0 ? (long long)block_frequency << (3 * (blocking_level - 1)) : 0;
+        if (block_frequency <= 0 || last > max_steps || lat->g.nx % f || lat->g.ny % f || lat->g.nz % f) {
+            tcym_set_error(lat->ctx, "tcym_cooling_create_ex: blocking level %d needs extents divisible by %d and "
+                                     "block_frequency * 8^(level-1) <= max_steps", blocking_level, f);
+            return TCYM_ERR_ARG;
+        }
+    }
     tcym_cooling c = new (std::nothrow) tcym_cooling_s;
     if (!c) return TCYM_ERR_OOM;
     c->hot = lat;
     c->max_steps = max_steps;
     c->sqrt_dctau = sqrt_dctau;
-    tcym_lattice *ls[3] = {&c->uold, &c->unew, &c->mid};
-    for (tcym_lattice *l : ls) {
-        int r = tcym_lattice_create_ex(lat->ctx, lat->nc, lat->g.nx, lat->g.ny, lat->g.nz, lat->a, lat->precision, l);
+    c->level = blocking_level;
+    c->block_frequency = block_frequency;
+    // UOld, UNew, UMid at the blocked extents (spacings are set by the Blocks); work lattices per level
+    std::vector<std::pair<tcym_lattice *, int>> ls = {{&c->uold, blocking_level}, {&c->unew, blocking_level},
+                                                      {&c->mid, blocking_level}};
+    for (int b = 0; b < blocking_level; ++b) ls.push_back({&c->work[b], b});
+    for (auto &[l, b] : ls) {
+        double a[3];
+        for (int i = 0; i < 3; ++i) a[i] = lat->a[i] * (1 << b);
+        int r = tcym_lattice_create_ex(lat->ctx, lat->nc, lat->g.nx >> b, lat->g.ny >> b, lat->g.nz >> b, a,
+                                       lat->precision, l);
         if (r) {
             tcym_cooling_destroy(c);
             return r;
@@ -134,11 +185,17 @@ extern "C" int tcym_cooling_create(tcym_lattice lat, int max_steps, double sqrt_
     return TCYM_OK;
 }
 
+extern "C" int tcym_cooling_create(tcym_lattice lat, int max_steps, double sqrt_dctau, tcym_cooling *out) {
+    return tcym_cooling_create_ex(lat, max_steps, sqrt_dctau, 0, 0, out);
+}
+
 extern "C" int tcym_cooling_destroy(tcym_cooling c) {
     if (!c) return TCYM_ERR_ARG;
     if (c->uold) tcym_lattice_destroy(c->uold);
     if (c->unew) tcym_lattice_destroy(c->unew);
     if (c->mid) tcym_lattice_destroy(c->mid);
+    for (tcym_lattice w : c->work)
+        if (w) tcym_lattice_destroy(w);
     delete c;
     return TCYM_OK;
 }
@@ -180,6 +237,14 @@ extern "C" int tcym_cooling_delta_ncs(tcym_cooling c, int norder, double *out) {
     if (!c->started) return TCYM_ERR_STATE;
     cudaSetDevice(c->hot->ctx->device);
     return delta_ncs(c, norder, out);
+}
+
+// the cooled links UOld (after start / update: the latest cooled copy) in the
+// reference's AoS layout, on the extents divided by 2^level
+extern "C" int tcym_cooling_links(tcym_cooling c, double *U_aos) {
+    if (!c || !U_aos) return TCYM_ERR_ARG;
+    if (!c->started) return TCYM_ERR_STATE;
+    return tcym_lattice_download(c->uold, U_aos, nullptr);
 }
 
 extern "C" int tcym_cooling_total(tcym_cooling c, double *out) {

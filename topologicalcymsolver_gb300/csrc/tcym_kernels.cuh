@@ -227,6 +227,10 @@ template <int FMT> __global__ void k_random_links(Geom g, void *U, double sigma,
     int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (s < g.V) site_random_links<Fmt<FMT>>(g, U, sigma, seed, s);
 }
+template <int FMT> __global__ void k_block(Geom gs, Geom gd, const void *Us, void *Ud) {
+    int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < gd.V) site_block<Fmt<FMT>>(gs, gd, Us, Ud, s);
+}
 template <int FMT> __global__ void k_reunitarize(Geom g, void *U) {
     int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (s < g.V) site_reunitarize<Fmt<FMT>>(g, U, s);
@@ -368,6 +372,11 @@ template <int FMT> struct Launch {
     static cudaError_t geodesic(const Geom &g, const void *Uold, const void *Unew, double c, void *Umid, void *Emid,
                                 cudaStream_t st) {
         k_geodesic<FMT><<<grid_for(g.V, 128), 128, 0, st>>>(g, Uold, Unew, c, Umid, Emid);
+        return cudaGetLastError();
+    }
+    // the blocked links of gs on gd (half the even extents)
+    static cudaError_t block(const Geom &gs, const Geom &gd, const void *Us, void *Ud, cudaStream_t st) {
+        k_block<FMT><<<grid_for(gd.V, 128), 128, 0, st>>>(gs, gd, Us, Ud);
         return cudaGetLastError();
     }
     static cudaError_t reunitarize(const Geom &g, void *U, cudaStream_t st) {

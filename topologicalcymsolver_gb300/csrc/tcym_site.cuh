@@ -535,6 +535,22 @@ template <class F> TCYM_HD void site_random_links(const Geom &g, void *U, double
     }
 }
 
+// Block (LATTICE/GaugeLinks.cpp:124-145) for site s of the blocked lattice gd
+// (half the even extents of gs): U'_mu(x) = U_mu(2x) U_mu(2x + mu), the product
+// in FP64 whatever the storage.
+template <class F> TCYM_HD void site_block(const Geom &gs, const Geom &gd, const void *Us, void *Ud, int64_t s) {
+    using T = typename F::T;
+    using G64 = Group64<F>;
+    const int x = (int)(s % gd.nx), y = (int)((s / gd.nx) % gd.ny), z = (int)(s / ((int64_t)gd.nx * gd.ny));
+    const int64_t s0 = 2 * x + (int64_t)gs.nx * (2 * y + (int64_t)gs.ny * (2 * z));
+    const int64_t step[3] = {1, gs.nx, (int64_t)gs.nx * gs.ny};  // 2x + mu stays inside: extents are even
+    for (int mu = 0; mu < 3; ++mu) {
+        const auto a = recast<double>(F::load(Us, gs.V, mu, s0));
+        const auto b = recast<double>(F::load(Us, gs.V, mu, s0 + step[mu]));
+        F::store(Ud, gd.V, mu, s, recast<T>(G64::mul(a, b)));
+    }
+}
+
 // FP64 reunitarisation of the stored links (new: the reference only monitors
 // unitarity).  Links are widened to FP64, projected and rounded back.
 template <class F> TCYM_HD void site_reunitarize(const Geom &g, void *U, int64_t s) {
