@@ -27,7 +27,20 @@ template <class T> struct Member {
     double ncs_dt;       // Kahan increment factor for measurements (0: no N_CS update)
 };
 
+// 1: the batched kernels walk their work items with a grid of the resident
+// blocks; 0: one block per work item
+#ifndef TCYM_BATCH_PERSISTENT
+#define TCYM_BATCH_PERSISTENT 0
+#endif
+// the batched step reading its coefficients from the member table holds more
+// than the single-lattice step: SU(2) at 7 blocks per SM (72 registers) spills
+// there, so it keeps its own target (the uniform-coefficient kernel takes the
+// single-lattice one)
+#ifndef TCYM_SU2_BATCH_MINBLOCKS
+#define TCYM_SU2_BATCH_MINBLOCKS 6
+#endif
 template <int FMT> constexpr int batch_min_blocks_for() {
+    if constexpr (Fmt<FMT>::PAIRED && Fmt<FMT>::NA == 3) return TCYM_SU2_BATCH_MINBLOCKS;
     return Fmt<FMT>::PAIRED ? pair_min_blocks_for<FMT>() : min_blocks_for<FMT>();
 }
 
@@ -88,6 +101,37 @@ __global__ void __launch_bounds__(threads_for<FMT>(), batch_min_blocks_for<FMT>(
     }
 }
 
+// The lean path when every member takes the same step coefficients (the same
+// mode, dt and spacings, no Langevin noise): they come from the kernel's
+// parameters, as in the single-lattice step, instead of from the member table
+// in memory at each use (the single-lattice kernel was 11% (SU(3)) and 29%
+// (SU(2)) faster than the table-reading one on the same 128^3 lattice).
+template <int FMT>
+__global__ void __launch_bounds__(kThreadsPair, pair_min_blocks_for<FMT>())
+    k_step_batch_uniform(const Member<float> *__restrict__ members, int nmembers, int total_blocks, int k,
+                         StepCoef<float> c) {
+    static_assert(Fmt<FMT>::PAIRED, "paired formats only");
+#if TCYM_BATCH_PERSISTENT
+    for (int item = blockIdx.x; item < total_blocks; item += gridDim.x) {
+#else
+    {  // one work item per block
+        const int item = blockIdx.x;
+        if (item >= total_blocks) return;
+#endif
+        const int mi = find_member(members, nmembers, item, false);
+        const Member<float> &m = members[mi];
+        const Geom g = m.g;
+        const int64_t p0 = (int64_t)(item - m.block_begin) * kThreadsPair, p = p0 + threadIdx.x;
+        if (p < (g.V >> 1)) {
+            const int in = m.cur ^ (k & 1);
+            if (pairs_touch_seam(g, p0, kThreadsPair))
+                site_step_pair<Fmt<FMT>, true>(g, m.U[in], m.U[in ^ 1], m.E, c, p, (uint64_t)k);
+            else
+                site_step_pair<Fmt<FMT>, false>(g, m.U[in], m.U[in ^ 1], m.E, c, p, (uint64_t)k);
+        }
+    }
+}
+
 // Observables of every member: one partial record per reduction work item.
 template <int FMT>
 __global__ void __launch_bounds__(kRedThreads)
@@ -143,11 +187,18 @@ template <int FMT> struct LaunchBatch {
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_step_batch<FMT, true>, TPB, 0);
         return b > 0 ? b : 1;
     }
-    // general: some member is unpaired or tiled (see k_step_batch)
+    // general: some member is unpaired or tiled (see k_step_batch); uniform: every
+    // member steps with the coefficients cu (k_step_batch_uniform)
     static cudaError_t step(const Member<T> *members, int n, int total_blocks, int k, int grid, bool general,
-                            cudaStream_t st) {
-        if (general || !Fmt<FMT>::PAIRED) k_step_batch<FMT, true><<<grid, TPB, 0, st>>>(members, n, total_blocks, k);
-        else k_step_batch<FMT, false><<<grid, TPB, 0, st>>>(members, n, total_blocks, k);
+                            bool uniform, const StepCoef<double> &cu, cudaStream_t st) {
+        if (general || !Fmt<FMT>::PAIRED) {
+            k_step_batch<FMT, true><<<grid, TPB, 0, st>>>(members, n, total_blocks, k);
+        } else if (uniform) {
+            if constexpr (Fmt<FMT>::PAIRED)
+                k_step_batch_uniform<FMT><<<grid, TPB, 0, st>>>(members, n, total_blocks, k, coef_cast<float>(cu));
+        } else {
+            k_step_batch<FMT, false><<<grid, TPB, 0, st>>>(members, n, total_blocks, k);
+        }
         return cudaGetLastError();
     }
     static cudaError_t observables(const Member<T> *members, int n, int total_blocks, int mask, double *partial,

@@ -20,13 +20,10 @@
 #include "tcym_batch.cuh"
 #include "tcym_internal.h"
 
-// 0 (default): one block per work item, scheduled by the hardware, so the
-// formats' launches interleave on the SMs and tails fill; 1: one wave of
-// resident blocks walking the work items (measured 6% slower on a 256-member
-// mixed ensemble).
-#ifndef TCYM_BATCH_PERSISTENT
-#define TCYM_BATCH_PERSISTENT 0
-#endif
+// TCYM_BATCH_PERSISTENT (tcym_batch.cuh) 0, the default: one block per work
+// item, scheduled by the hardware, so the formats' launches interleave on the
+// SMs and tails fill; 1: one wave of resident blocks walking the work items
+// (measured 6% slower on a 256-member mixed ensemble).
 
 using namespace tcym;
 
@@ -46,6 +43,8 @@ struct FmtGroup {
     std::vector<char> h_members; // host copy of the table
     int total_blocks = 0, red_total = 0, grid = 0, red_grid = 0, red_offset = 0;
     bool general = false;        // some member is unpaired or tiled: the general batch kernel
+    bool uniform = false;        // every member steps with coef (no Langevin noise)
+    StepCoef<double> coef{};
 };
 
 int fail(tcym_ctx ctx, cudaError_t e, const char *w) {
@@ -92,7 +91,15 @@ template <int FMT> static void fill_group(tcym_ensemble ens, FmtGroup &G, int sm
         m.U[1] = L->U[1];
         m.E = L->E;
         m.result = L->result;
-        m.c = coef_cast<T>(tcym_coef(L->a, em.mode, em.dt, em.gamma, em.T, em.seed, em.next_step));
+        const StepCoef<double> cd = tcym_coef(L->a, em.mode, em.dt, em.gamma, em.T, em.seed, em.next_step);
+        m.c = coef_cast<T>(cd);
+        if (i == 0) {
+            G.coef = cd;
+            G.uniform = cd.mode != MODE_LANGEVIN;
+        } else if (cd.mode != G.coef.mode || std::memcmp(cd.fc, G.coef.fc, sizeof cd.fc) ||
+                   std::memcmp(cd.cnu, G.coef.cnu, sizeof cd.cnu) || std::memcmp(cd.uc, G.coef.uc, sizeof cd.uc)) {
+            G.uniform = false;
+        }
         m.cur = L->cur;
         m.block_begin = blk;
         m.paired = Fmt<FMT>::PAIRED && L->g.nz % 2 == 0;
@@ -104,6 +111,7 @@ template <int FMT> static void fill_group(tcym_ensemble ens, FmtGroup &G, int sm
         red += m.red_blocks;
         m.ncs_dt = 0.0;
     }
+    if (G.idx.empty()) G.uniform = false;
     G.total_blocks = blk;
     G.red_total = red;
 #if TCYM_BATCH_PERSISTENT
@@ -177,7 +185,7 @@ template <int FMT> static cudaError_t launch_group_step(tcym_ensemble ens, int f
     using T = typename Fmt<FMT>::T;
     const FmtGroup &G = ens->groups[f];
     return LaunchBatch<FMT>::step(static_cast<const Member<T> *>(G.d_members), (int)G.idx.size(), G.total_blocks, k,
-                                  G.grid, G.general, s);
+                                  G.grid, G.general, G.uniform, G.coef, s);
 }
 
 static cudaError_t group_step(tcym_ensemble ens, int f, int k, cudaStream_t s) {
