@@ -102,10 +102,11 @@ __global__ void __launch_bounds__(threads_for<FMT>(), batch_min_blocks_for<FMT>(
 }
 
 // The lean path when every member takes the same step coefficients (the same
-// mode, dt and spacings, no Langevin noise): they come from the kernel's
-// parameters, as in the single-lattice step, instead of from the member table
-// in memory at each use (the single-lattice kernel was 11% (SU(3)) and 29%
-// (SU(2)) faster than the table-reading one on the same 128^3 lattice).
+// mode, dt and spacings): they come from the kernel's parameters, as in the
+// single-lattice step, instead of from the member table in memory at each use
+// (the single-lattice kernel was 11% (SU(3)) and 29% (SU(2)) faster than the
+// table-reading one on the same 128^3 lattice).  Langevin noise coefficients
+// (seed, step, damping and kick, per member) still come from the table.
 template <int FMT>
 __global__ void __launch_bounds__(kThreadsPair, pair_min_blocks_for<FMT>())
     k_step_batch_uniform(const Member<float> *__restrict__ members, int nmembers, int total_blocks, int k,
@@ -125,9 +126,9 @@ __global__ void __launch_bounds__(kThreadsPair, pair_min_blocks_for<FMT>())
         if (p < (g.V >> 1)) {
             const int in = m.cur ^ (k & 1);
             if (pairs_touch_seam(g, p0, kThreadsPair))
-                site_step_pair<Fmt<FMT>, true>(g, m.U[in], m.U[in ^ 1], m.E, c, p, (uint64_t)k);
+                site_step_pair<Fmt<FMT>, true>(g, m.U[in], m.U[in ^ 1], m.E, c, m.c, p, (uint64_t)k);
             else
-                site_step_pair<Fmt<FMT>, false>(g, m.U[in], m.U[in ^ 1], m.E, c, p, (uint64_t)k);
+                site_step_pair<Fmt<FMT>, false>(g, m.U[in], m.U[in ^ 1], m.E, c, m.c, p, (uint64_t)k);
         }
     }
 }

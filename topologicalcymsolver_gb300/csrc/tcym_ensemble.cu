@@ -43,7 +43,7 @@ struct FmtGroup {
     std::vector<char> h_members; // host copy of the table
     int total_blocks = 0, red_total = 0, grid = 0, red_grid = 0, red_offset = 0;
     bool general = false;        // some member is unpaired or tiled: the general batch kernel
-    bool uniform = false;        // every member steps with coef (no Langevin noise)
+    bool uniform = false;        // every member steps with coef's mode, force, staple and link factors
     StepCoef<double> coef{};
 };
 
@@ -95,7 +95,7 @@ template <int FMT> static void fill_group(tcym_ensemble ens, FmtGroup &G, int sm
         m.c = coef_cast<T>(cd);
         if (i == 0) {
             G.coef = cd;
-            G.uniform = cd.mode != MODE_LANGEVIN;
+            G.uniform = true;
         } else if (cd.mode != G.coef.mode || std::memcmp(cd.fc, G.coef.fc, sizeof cd.fc) ||
                    std::memcmp(cd.cnu, G.coef.cnu, sizeof cd.cnu) || std::memcmp(cd.uc, G.coef.uc, sizeof cd.uc)) {
             G.uniform = false;

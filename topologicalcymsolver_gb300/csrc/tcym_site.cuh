@@ -151,9 +151,12 @@ TCYM_COLD void langevin_kick_pair(const StepCoef<float> &c, int mu, int64_t p, i
     for (int a = 0; a < NA; ++a) e[a] = e[a] + fma(kick, f2(x0[a], x1[a]), fma(-damp, e[a], fc * f[a]));
 }
 
+// cn: the Langevin noise's coefficients (seed, step, damping, kick), which may
+// sit apart from the step's (a batched member's own, beside coefficients the
+// members share)
 template <class F, bool SEAM>
-TCYM_HD void site_step_pair(const Geom &g, const void *Uin, void *Uout, void *E, const StepCoef<float> &c, int64_t p,
-                            uint64_t step_add = 0) {
+TCYM_HD void site_step_pair(const Geom &g, const void *Uin, void *Uout, void *E, const StepCoef<float> &c,
+                            const StepCoef<float> &cn, int64_t p, uint64_t step_add) {
     using G2 = typename F::G2;
     using M2 = typename F::Mat2;
     constexpr int NA = F::NA;
@@ -178,7 +181,7 @@ TCYM_HD void site_step_pair(const Geom &g, const void *Uin, void *Uout, void *E,
         G2::proj_mul(u, A, f);
         const f2 fc(sel3(c.fc, mu));
         if (c.mode == MODE_LANGEVIN) {
-            langevin_kick_pair<NA>(c, mu, p, Vh, step_add, fc, f, e);
+            langevin_kick_pair<NA>(cn, mu, p, Vh, step_add, fc, f, e);
         } else if (c.mode == MODE_FLOW) {
 #pragma unroll
             for (int a = 0; a < NA; ++a) e[a] = fc * f[a];
@@ -189,6 +192,12 @@ TCYM_HD void site_step_pair(const Geom &g, const void *Uin, void *Uout, void *E,
         F::store_e2(E, Vh, mu, p, e);
         F::store2(Uout, Vh, mu, p, G2::iexp_mul(f2(sel3(c.uc, mu)), e, u));
     }
+}
+
+template <class F, bool SEAM>
+TCYM_HD void site_step_pair(const Geom &g, const void *Uin, void *Uout, void *E, const StepCoef<float> &c, int64_t p,
+                            uint64_t step_add = 0) {
+    site_step_pair<F, SEAM>(g, Uin, Uout, E, c, c, p, step_add);
 }
 
 // Does the block of pairs [p0, p0 + n) touch the seam planes z = 0 or z = nz/2 - 1?
