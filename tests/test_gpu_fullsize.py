@@ -1,0 +1,120 @@
+"""Full-size checks through size-independent properties (the oracle is too slow
+at these sizes): the bench workload, SU(3) 128^3 from its own initial state, and
+a 256^3 lattice.
+
+* FP32 storage against the FP64 device path (itself checked against the oracle
+  at small sizes) pointwise over 20 leapfrog steps at 128^3, 1e-5 relative.
+* Over 300 steps at 128^3 (FP64 reunitarisation every 100): no energy drift
+  once the start has relaxed, the Gauss-law violation (conserved by the exact
+  dynamics) stays at FP32 rounding, the links stay unitary.
+* 256^3 (16.8 M sites, 8.4 M site pairs in 65,536 blocks): a few steps conserve the
+  Gauss violation and keep the links unitary.
+* tcym_leapfrog_host at 96^3 with the library's chunking equals the three
+  calls upload + step + download bit for bit.
+"""
+import math
+
+import numpy as np
+import pytest
+
+import topologicalcymsolver_gb300 as tcym
+
+pytestmark = pytest.mark.gpu
+
+
+def bench_state(ctx, L, precision):
+    """The bench's initial state: links exp(i theta t), theta ~ N(0, 0.09) (seed 2),
+    E ~ N(0, 1/2) (seed 1), Gauss-restored in FP64, stored in `precision`."""
+    ic = tcym.Lattice(ctx, 3, (L, L, L), tcym.FP64)
+    ic.random_links(0.3, 2)
+    ic.gaussian_efield(math.sqrt(0.5), 1)
+    ic.gauss_restore(1e-10, 5000)
+    if precision == tcym.FP64:
+        return ic
+    lat = tcym.Lattice(ctx, 3, (L, L, L), precision)
+    lat.copy_from(ic)
+    ic.close()
+    return lat
+
+
+def rel(a, b):
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+
+def test_fp32_against_fp64_at_128(ctx):
+    l64 = bench_state(ctx, 128, tcym.FP64)
+    l32 = tcym.Lattice(ctx, 3, (128, 128, 128), tcym.FP32)
+    l32.copy_from(l64)
+    for lat in (l32, l64):
+        lat.set_reunitarize_period(0)
+    l32.leapfrog(0.05, 20)
+    l64.leapfrog(0.05, 20)
+    U32, E32 = l32.download()
+    U64, E64 = l64.download()
+    assert rel(U32, U64) < 1e-5 and rel(E32, E64) < 1e-5, (rel(U32, U64), rel(E32, E64))
+    o32, o64 = l32.observables(), l64.observables()
+    assert abs(o32.T00 - o64.T00) < 1e-5 * abs(o64.T00)
+    assert abs(o32.edotb - o64.edotb) < 1e-4 * max(1.0, abs(o64.edotb))
+
+
+def test_conservation_at_128(ctx):
+    """300 steps: the measured energy (E half a step off the links) carries an O(dt)
+    offset that settles while this non-equilibrium start relaxes (about 100 steps),
+    after which symplectic leapfrog shows no drift."""
+    lat = bench_state(ctx, 128, tcym.FP32)
+    lat.set_reunitarize_period(100)
+    o0 = lat.observables()
+    energies = []
+    gauss = []
+    for _ in range(15):
+        lat.leapfrog(0.05, 20)
+        o = lat.observables()
+        energies.append(o.T00)
+        gauss.append(o.gauss_absmax)
+        assert not o.nonfinite
+    energies = np.array(energies)
+    assert np.abs(energies - o0.T00).max() < 1e-2 * abs(o0.T00), (o0.T00, energies)
+    late = energies[5:]  # after 100 steps
+    assert abs(late[5:].mean() - late[:5].mean()) < 2e-4 * abs(o0.T00), energies
+    # Gauss law: conserved by the dynamics; FP32 storage rounding only
+    assert max(gauss) < 1e-4, gauss
+    assert lat.observables().unit_max < 1e-5
+
+
+def test_conservation_at_256(ctx):
+    L = 256
+    lat = tcym.Lattice(ctx, 3, (L, L, L), tcym.FP32)
+    lat.random_links(0.3, 2)
+    lat.gaussian_efield(math.sqrt(0.5), 1)
+    lat.set_reunitarize_period(0)
+    o0 = lat.observables()
+    lat.leapfrog(0.05, 10)
+    o1 = lat.observables()
+    assert not o1.nonfinite
+    # the measured energy's O(dt) offset (E half a step off the links) moves while
+    # this unrelaxed start evolves; drift is checked at 128^3
+    assert abs(o1.T00 - o0.T00) < 2e-2 * abs(o0.T00), (o0.T00, o1.T00)
+    # unrestored fields: the violation is large but conserved
+    assert abs(o1.gauss_rms - o0.gauss_rms) < 1e-4 * o0.gauss_rms, (o0.gauss_rms, o1.gauss_rms)
+    assert o1.unit_max < 1e-5
+
+
+def test_host_step_at_96_equals_three_calls(ctx, monkeypatch):
+    torch = pytest.importorskip("torch")
+    monkeypatch.delenv("TCYM_HOST_STEP_CHUNK", raising=False)
+    L = 96
+    V = L ** 3
+    lat = bench_state(ctx, L, tcym.FP32)
+    lat.set_reunitarize_period(0)
+    U = torch.empty((V, 3, 18), dtype=torch.float64, pin_memory=True).numpy()
+    E = torch.empty((V, 3, 8), dtype=torch.float64, pin_memory=True).numpy()
+    lat.download(U, E)
+    ref = tcym.Lattice(ctx, 3, (L, L, L), tcym.FP32)
+    ref.set_reunitarize_period(0)
+    Ur, Er = U.copy(), E.copy()
+    for _ in range(3):
+        lat.leapfrog_host(0.05, U, E, U, E)
+        ref.upload(Ur, Er)
+        ref.leapfrog(0.05, 1)
+        Ur, Er = ref.download()
+    assert np.array_equal(U, Ur) and np.array_equal(E, Er)
