@@ -125,7 +125,7 @@ int tcym_leapfrog_host(tcym_lattice lat, double dt, const double *U_in, const do
  * U'_mu(x) = U_mu(2x) U_mu(2x + mu) (products in FP64), its fields zero and its
  * spacings twice src's. */
 int tcym_lattice_block(const tcym_lattice src, tcym_lattice dst);
-/* dst <- src (same group and extents; any precisions): Copy() of GaugeLinks.cpp:91-107
+/* dst <- src: links, fields and spacings (same group and extents; any precisions): Copy() of GaugeLinks.cpp:91-107
  * and ElectricFields.cpp:90-104. */
 int tcym_lattice_copy(tcym_lattice dst, const tcym_lattice src);
 /* Waits for all work queued on the lattice. */

@@ -378,6 +378,11 @@ extern "C" int tcym_lattice_copy(tcym_lattice dst, const tcym_lattice src) {
         DISPATCH(src->fmt, CK(L::to_aos(src->g, src->U[src->cur], src->E, du, de, dst->stream)));
         DISPATCH(dst->fmt, CK(L::from_aos(dst->g, dst->U[dst->cur], dst->E, du, de, dst->stream)));
     }
+    // the spacings too, as Copy does (GaugeLinks.cpp:91-100)
+    if (std::memcmp(dst->a, src->a, sizeof dst->a) != 0) {
+        std::memcpy(dst->a, src->a, sizeof dst->a);
+        drop_host_graphs(dst);  // their step coefficients hold the old spacings
+    }
     CK(cudaStreamSynchronize(dst->stream));
     return TCYM_OK;
 }
