@@ -40,7 +40,8 @@ def load():
         L.hc_normal.argtypes = [ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32,
                                 ctypes.c_uint32, ctypes.c_int]
         L.hc_normal.restype = ctypes.c_double
-        L.hc_pipeline_schedule.argtypes = [ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, _vp, _vp, ctypes.c_int64]
+        L.hc_pipeline_schedule.argtypes = [ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, _vp, ctypes.c_int64, _vp,
+                                           _vp, ctypes.c_int64]
         L.hc_pipeline_schedule.restype = ctypes.c_int64
         _L = L
     return _L
@@ -140,10 +141,12 @@ def normal(seed, stream, step, site, mu, a, single=False):
 
 
 def pipeline_schedule(N, P, C):
-    """[(kind, chunk)] of the host-resident step's pipeline (0 upload, 1 step)."""
+    """(bounds, [(kind, chunk)]) of the host-resident step's pipeline (0 upload, 1 step)."""
     L = load()
-    cap = 4 * ((N + C - 1) // C) + 4
-    kinds, chunks = np.zeros(cap, np.int32), np.zeros(cap, np.int64)
-    n = L.hc_pipeline_schedule(N, P, C, _p(kinds), _p(chunks), cap)
-    assert n <= cap
-    return list(zip(kinds[:n].tolist(), chunks[:n].tolist()))
+    cap = 4 * ((N + 127) // 128) + 16
+    bounds = np.zeros(cap, np.int64)
+    kinds, chunks = np.zeros(2 * cap, np.int32), np.zeros(2 * cap, np.int64)
+    n = L.hc_pipeline_schedule(N, P, C, _p(bounds), cap, _p(kinds), _p(chunks), 2 * cap)
+    assert n <= 2 * cap
+    nchunks = n // 2
+    return bounds[:nchunks + 1].tolist(), list(zip(kinds[:n].tolist(), chunks[:n].tolist()))

@@ -29,21 +29,24 @@ def stencil_max(nx, ny, nzp, a, b):
 
 def check_schedule(nx, ny, nzp, C):
     N, P = nx * ny * nzp, nx * ny
-    ops = hc.pipeline_schedule(N, P, C)
-    n = (N + C - 1) // C
+    b, ops = hc.pipeline_schedule(N, P, C)
+    n = len(b) - 1
+    assert b[0] == 0 and b[-1] == N and all(x < y for x, y in zip(b, b[1:]))
+    assert all(x % 128 == 0 for x in b[:-1])  # the paired step's blocks start on chunk bounds
+    assert all(y - x <= max(C, 128) for x, y in zip(b, b[1:]))
     assert sorted(j for k, j in ops if k == 0) == list(range(n))
     assert sorted(j for k, j in ops if k == 1) == list(range(n))
     up = 0  # uploads are in chunk order, so the units on the device are [0, up)
     expect_next = 0
     for kind, j in ops:
-        a, b = j * C, min(N, (j + 1) * C)
+        lo, hi = b[j], b[j + 1]
         if kind == 0:
             assert j == expect_next
             expect_next += 1
-            up = b
+            up = hi
             continue
-        assert stencil_max(nx, ny, nzp, a, b) < up, (nx, ny, nzp, C, j, up)
-    return ops
+        assert stencil_max(nx, ny, nzp, lo, hi) < up, (nx, ny, nzp, C, j, up)
+    return b, ops
 
 
 @pytest.mark.parametrize("nx,ny,nz", [(8, 8, 12), (8, 8, 9), (16, 16, 8), (12, 10, 14), (5, 6, 7), (128, 128, 128),
@@ -57,10 +60,15 @@ def test_schedule_respects_neighbourhoods(nx, ny, nz, paired, C):
 
 
 def test_schedule_overlaps_steps_with_uploads():
-    """At 128^3 (paired, 64 MB chunks) steps start long before the last upload:
-    the transfer directions overlap."""
-    ops = check_schedule(128, 128, 64, 53760)
+    """At 128^3 (paired, 64 MB chunks): one-plane chunks at both ends, so stepping
+    starts after four planes are up and little is left to download after the
+    last upload; steps start long before the last upload."""
+    b, ops = check_schedule(128, 128, 64, 53760)
+    P = 128 * 128
     first_step = next(i for i, (k, _) in enumerate(ops) if k == 1)
+    uploads_before = sum(1 for k, _ in ops[:first_step] if k == 0)
+    assert b[uploads_before] <= 4 * P
     last_upload = max(i for i, (k, _) in enumerate(ops) if k == 0)
-    n = (128 ** 3 // 2 + 53759) // 53760
-    assert first_step < 6 and last_upload > n  # stepping starts within the first few uploads
+    left = [j for k, j in ops[last_upload + 1:] if k == 1]
+    assert sum(b[j + 1] - b[j] for j in left) <= 4 * P  # the last two planes' chunks and the first plane's
+    assert last_upload > len(b)  # steps interleave with uploads

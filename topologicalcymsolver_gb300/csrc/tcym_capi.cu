@@ -629,9 +629,10 @@ static cudaError_t host_step_pipeline(tcym_lattice lat, const StepCoef<double> &
         if (err == cudaSuccess) err = cudaEventRecord(e, from);
         if (err == cudaSuccess) err = cudaStreamWaitEvent(to, e, 0);
     };
-    pipeline_schedule(N, P, C, [&](int op, int64_t j) {
+    const std::vector<int64_t> bounds = pipeline_bounds(N, P, C);
+    pipeline_schedule(bounds, P, [&](int op, int64_t j) {
         if (err != cudaSuccess) return;
-        const int64_t a = j * C, n = ((j + 1) * C < N ? (j + 1) * C : N) - a;
+        const int64_t a = bounds[j], n = bounds[j + 1] - a;
         if (op == PIPE_UPLOAD) {
             copy(du, U_in, a, n, nmd, cudaMemcpyHostToDevice, cin);
             copy(de, E_in, a, n, na, cudaMemcpyHostToDevice, cin);

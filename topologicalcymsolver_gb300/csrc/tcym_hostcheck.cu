@@ -238,11 +238,15 @@ int hc_iexp(int fmt, double c, const double *alpha, double *out) {
     HC_DISPATCH(fmt, HH::iexp_aos(c, alpha, out));
     return 0;
 }
-// the issue order of the host-resident step's pipeline: kinds[i] (0 upload,
-// 1 step) of chunks[i]; returns the number of operations (at most cap written)
-int64_t hc_pipeline_schedule(int64_t N, int64_t P, int64_t C, int *kinds, int64_t *chunks, int64_t cap) {
+// the host-resident step's pipeline for N units in planes of P, chunk size C:
+// its chunk bounds (at most cap written) and the issue order, kinds[i] (0
+// upload, 1 step) of chunks[i]; returns the number of operations
+int64_t hc_pipeline_schedule(int64_t N, int64_t P, int64_t C, int64_t *bounds, int64_t bcap, int *kinds,
+                             int64_t *chunks, int64_t cap) {
+    const std::vector<int64_t> b = pipeline_bounds(N, P, C);
+    for (int64_t i = 0; i < (int64_t)b.size() && i < bcap; ++i) bounds[i] = b[i];
     int64_t n = 0;
-    pipeline_schedule(N, P, C, [&](int op, int64_t j) {
+    pipeline_schedule(b, P, [&](int op, int64_t j) {
         if (n < cap) { kinds[n] = op; chunks[n] = j; }
         ++n;
     });
