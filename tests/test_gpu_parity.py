@@ -1,6 +1,6 @@
 """GPU parity: the sm_103a kernels through the C ABI against the FP64 oracle.
 
-Tolerances (spec contract): FP64 device path <= 1e-10 relative over short
+Tolerances (the accuracy contract): FP64 device path <= 1e-10 relative over short
 windows (<= 100 steps), FP32 storage path <= 1e-5 relative.  "Relative" is the
 max-abs difference over the max-abs magnitude of the oracle's array.
 """
