@@ -118,3 +118,25 @@ def test_host_step_at_96_equals_three_calls(ctx, monkeypatch):
         ref.leapfrog(0.05, 1)
         Ur, Er = ref.download()
     assert np.array_equal(U, Ur) and np.array_equal(E, Er)
+
+
+@pytest.mark.parametrize("prec", [pytest.param(tcym.FP32, id="fp32"), pytest.param(tcym.FP64, id="fp64")])
+def test_energy_drift_1e4_steps_at_128(ctx, prec):
+    """10^4 leapfrog steps of the bench workload (FP32: FP64 reunitarisation every
+    100): the energy, sampled every 100 steps after the first 1000, changes by
+    |dE/E| <= 1e-6 between the halves of the run (the sample mean's standard error
+    is about 1e-6 at this volume), and a linear fit drifts by at most a few 1e-6."""
+    lat = bench_state(ctx, 128, prec)
+    lat.set_reunitarize_period(100 if prec == tcym.FP32 else 0)
+    e0 = lat.observables().T00
+    e = []
+    for _ in range(100):
+        lat.leapfrog(0.05, 100)
+        e.append(lat.observables().T00)
+    late = np.array(e[10:])
+    half = len(late) // 2
+    halves = (late[half:].mean() - late[:half].mean()) / e0
+    fit = np.polyfit(np.arange(len(late)) * 100.0, late, 1)[0] * 1e4 / e0
+    sem = late.std() / np.sqrt(len(late)) / e0
+    print(f"dE/E halves {halves:.2e}, fit over 1e4 steps {fit:.2e}, standard error {sem:.2e}")
+    assert abs(halves) <= 2e-6 and abs(fit) <= 6e-6, (halves, fit, sem)
