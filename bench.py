@@ -79,6 +79,18 @@ def dist_env():
     return ws, rank, local
 
 
+def max_over_ranks(x, device):
+    """x's maximum over the ranks of the default process group (x alone without one):
+    each rank times its own replica, and the job takes as long as the slowest."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return x
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def measured_peak():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -235,11 +247,8 @@ def run_ours(a):
     per = [ev[k].elapsed_time(ev[k + 1]) * 1e-3 for k in range(a.steps)]
     total = ev[0].elapsed_time(ev[-1]) * 1e-3
     reunits = sum(1 for s in range(steps_before + 1, steps_before + a.steps + 1) if s % 100 == 0)
-    if ws > 1:
-        t = torch.tensor([total], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total = float(t.item())
-    value = ws * links * a.steps / total
+    total = max_over_ranks(total, "cuda")
+    value = ws * links * a.steps / total  # the units all ranks processed over the slowest rank's time
 
     # ---- end to end through the C ABI with pinned host buffers: the state lives in
     # host memory and every step moves it in and out (updated in place, a trajectory)
@@ -256,12 +265,7 @@ def run_ours(a):
         t0 = time.perf_counter()
         for _ in range(n_e2e):
             fn()
-        el = time.perf_counter() - t0
-        if ws > 1:
-            t = torch.tensor([el], device="cuda")
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            el = float(t.item())
-        return ws * links * n_e2e / el
+        return ws * links * n_e2e / max_over_ranks(time.perf_counter() - t0, "cuda")
 
     def three_calls():
         lat.upload(Uh, Eh)
