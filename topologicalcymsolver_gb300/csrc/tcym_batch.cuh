@@ -107,16 +107,18 @@ __global__ void __launch_bounds__(threads_for<FMT>(), batch_min_blocks_for<FMT>(
 // (the single-lattice kernel was 11% (SU(3)) and 29% (SU(2)) faster than the
 // table-reading one on the same 128^3 lattice).  Langevin noise coefficients
 // (seed, step, damping and kick, per member) still come from the table.
+// The members are a slice of a format's table (one coefficient class), whose
+// work items run from item0 to total_blocks.
 template <int FMT>
 __global__ void __launch_bounds__(kThreadsPair, pair_min_blocks_for<FMT>())
-    k_step_batch_uniform(const Member<float> *__restrict__ members, int nmembers, int total_blocks, int k,
+    k_step_batch_uniform(const Member<float> *__restrict__ members, int nmembers, int item0, int total_blocks, int k,
                          StepCoef<float> c) {
     static_assert(Fmt<FMT>::PAIRED, "paired formats only");
 #if TCYM_BATCH_PERSISTENT
-    for (int item = blockIdx.x; item < total_blocks; item += gridDim.x) {
+    for (int item = item0 + blockIdx.x; item < total_blocks; item += gridDim.x) {
 #else
     {  // one work item per block
-        const int item = blockIdx.x;
+        const int item = item0 + blockIdx.x;
         if (item >= total_blocks) return;
 #endif
         const int mi = find_member(members, nmembers, item, false);
@@ -188,19 +190,23 @@ template <int FMT> struct LaunchBatch {
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_step_batch<FMT, true>, TPB, 0);
         return b > 0 ? b : 1;
     }
-    // general: some member is unpaired or tiled (see k_step_batch); uniform: every
-    // member steps with the coefficients cu (k_step_batch_uniform)
+    // general: some member is unpaired or tiled (see k_step_batch)
     static cudaError_t step(const Member<T> *members, int n, int total_blocks, int k, int grid, bool general,
-                            bool uniform, const StepCoef<double> &cu, cudaStream_t st) {
-        if (general || !Fmt<FMT>::PAIRED) {
-            k_step_batch<FMT, true><<<grid, TPB, 0, st>>>(members, n, total_blocks, k);
-        } else if (uniform) {
-            if constexpr (Fmt<FMT>::PAIRED)
-                k_step_batch_uniform<FMT><<<grid, TPB, 0, st>>>(members, n, total_blocks, k, coef_cast<float>(cu));
-        } else {
-            k_step_batch<FMT, false><<<grid, TPB, 0, st>>>(members, n, total_blocks, k);
-        }
+                            cudaStream_t st) {
+        if (general || !Fmt<FMT>::PAIRED) k_step_batch<FMT, true><<<grid, TPB, 0, st>>>(members, n, total_blocks, k);
+        else k_step_batch<FMT, false><<<grid, TPB, 0, st>>>(members, n, total_blocks, k);
         return cudaGetLastError();
+    }
+    // the members [m0, m0 + n) of one coefficient class, work items [item0, item1),
+    // stepped with their shared coefficients cu (k_step_batch_uniform)
+    static cudaError_t step_uniform(const Member<T> *members, int m0, int n, int item0, int item1, int k,
+                                    const StepCoef<double> &cu, cudaStream_t st) {
+        if constexpr (Fmt<FMT>::PAIRED) {
+            k_step_batch_uniform<FMT><<<item1 - item0, TPB, 0, st>>>(members + m0, n, item0, item1, k,
+                                                                    coef_cast<float>(cu));
+            return cudaGetLastError();
+        }
+        return cudaErrorInvalidValue;
     }
     static cudaError_t observables(const Member<T> *members, int n, int total_blocks, int mask, double *partial,
                                    int grid, cudaStream_t st) {

@@ -14,6 +14,7 @@
 #include <algorithm>
 #include <cstring>
 #include <new>
+#include <tuple>
 #include <vector>
 
 #include "../../include/tcym.h"
@@ -43,8 +44,13 @@ struct FmtGroup {
     std::vector<char> h_members; // host copy of the table
     int total_blocks = 0, red_total = 0, grid = 0, red_grid = 0, red_offset = 0;
     bool general = false;        // some member is unpaired or tiled: the general batch kernel
-    bool uniform = false;        // every member steps with coef's mode, force, staple and link factors
-    StepCoef<double> coef{};
+    // runs of members (idx is ordered by coefficients) that share the mode, force, staple
+    // and link factors: each steps in one launch with them as kernel parameters
+    struct Class {
+        StepCoef<double> coef;
+        int m0, m1, item0, item1;
+    };
+    std::vector<Class> classes;
 };
 
 int fail(tcym_ctx ctx, cudaError_t e, const char *w) {
@@ -82,6 +88,7 @@ template <int FMT> static void fill_group(tcym_ensemble ens, FmtGroup &G, int sm
     std::vector<Member<T>> tab(G.idx.size());
     int blk = 0, red = 0;
     G.general = false;
+    G.classes.clear();
     for (size_t i = 0; i < G.idx.size(); ++i) {
         const EnsMember &em = ens->members[G.idx[i]];
         const tcym_lattice L = em.lat;
@@ -93,25 +100,23 @@ template <int FMT> static void fill_group(tcym_ensemble ens, FmtGroup &G, int sm
         m.result = L->result;
         const StepCoef<double> cd = tcym_coef(L->a, em.mode, em.dt, em.gamma, em.T, em.seed, em.next_step);
         m.c = coef_cast<T>(cd);
-        if (i == 0) {
-            G.coef = cd;
-            G.uniform = true;
-        } else if (cd.mode != G.coef.mode || std::memcmp(cd.fc, G.coef.fc, sizeof cd.fc) ||
-                   std::memcmp(cd.cnu, G.coef.cnu, sizeof cd.cnu) || std::memcmp(cd.uc, G.coef.uc, sizeof cd.uc)) {
-            G.uniform = false;
-        }
+        const FmtGroup::Class *last = G.classes.empty() ? nullptr : &G.classes.back();
+        if (!last || cd.mode != last->coef.mode || std::memcmp(cd.fc, last->coef.fc, sizeof cd.fc) ||
+            std::memcmp(cd.cnu, last->coef.cnu, sizeof cd.cnu) || std::memcmp(cd.uc, last->coef.uc, sizeof cd.uc))
+            G.classes.push_back(FmtGroup::Class{cd, (int)i, (int)i, blk, blk});
         m.cur = L->cur;
         m.block_begin = blk;
         m.paired = Fmt<FMT>::PAIRED && L->g.nz % 2 == 0;
         m.tile = m.paired ? tcym_lattice_tile_of(L) : Tile{0, 0, 0, 0, 0, 0};
         if (!m.paired || m.tile.tx != 0) G.general = true;
         blk += m.paired ? (int)tile_blocks(L->g, m.tile) : grid_for(L->g.V, TPB);
+        G.classes.back().m1 = (int)i + 1;
+        G.classes.back().item1 = blk;
         m.red_begin = red;
         m.red_blocks = grid_for(L->g.V, kRedThreads);
         red += m.red_blocks;
         m.ncs_dt = 0.0;
     }
-    if (G.idx.empty()) G.uniform = false;
     G.total_blocks = blk;
     G.red_total = red;
 #if TCYM_BATCH_PERSISTENT
@@ -127,6 +132,13 @@ template <int FMT> static void fill_group(tcym_ensemble ens, FmtGroup &G, int sm
 static void fill_all(tcym_ensemble ens) {
     for (int f = 0; f < 4; ++f) ens->groups[f].idx.clear();
     for (size_t i = 0; i < ens->members.size(); ++i) ens->groups[ens->members[i].lat->fmt].idx.push_back((int)i);
+    // members with the same step coefficients next to each other (mode, dt, spacings decide them)
+    for (auto &G : ens->groups)
+        std::stable_sort(G.idx.begin(), G.idx.end(), [&](int x, int y) {
+            const EnsMember &a = ens->members[x], &b = ens->members[y];
+            return std::make_tuple(a.mode, a.dt, a.lat->a[0], a.lat->a[1], a.lat->a[2]) <
+                   std::make_tuple(b.mode, b.dt, b.lat->a[0], b.lat->a[1], b.lat->a[2]);
+        });
     const int sm = ens->ctx->sm_count;
     fill_group<FMT_SU2_F32>(ens, ens->groups[FMT_SU2_F32], sm);
     fill_group<FMT_SU2_F64>(ens, ens->groups[FMT_SU2_F64], sm);
@@ -184,8 +196,14 @@ static int upload_tables(tcym_ensemble ens) {
 template <int FMT> static cudaError_t launch_group_step(tcym_ensemble ens, int f, int k, cudaStream_t s) {
     using T = typename Fmt<FMT>::T;
     const FmtGroup &G = ens->groups[f];
-    return LaunchBatch<FMT>::step(static_cast<const Member<T> *>(G.d_members), (int)G.idx.size(), G.total_blocks, k,
-                                  G.grid, G.general, G.uniform, G.coef, s);
+    const Member<T> *table = static_cast<const Member<T> *>(G.d_members);
+    if (!Fmt<FMT>::PAIRED || G.general)
+        return LaunchBatch<FMT>::step(table, (int)G.idx.size(), G.total_blocks, k, G.grid, G.general, s);
+    for (const FmtGroup::Class &c : G.classes) {
+        const cudaError_t e = LaunchBatch<FMT>::step_uniform(table, c.m0, c.m1 - c.m0, c.item0, c.item1, k, c.coef, s);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
 }
 
 static cudaError_t group_step(tcym_ensemble ens, int f, int k, cudaStream_t s) {
