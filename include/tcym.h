@@ -133,6 +133,11 @@ int tcym_lattice_sync(tcym_lattice lat);
 /* The lattice's CUDA stream (a cudaStream_t), for ordering or timing caller work
  * against the library's kernels. */
 int tcym_lattice_stream(tcym_lattice lat, void **stream);
+/* Page-locked host memory (cudaMallocHost) for the host arrays of tcym_lattice_upload / _download and
+ * tcym_leapfrog_host, whose copies then run asynchronously (and, for the host-resident step, overlap
+ * each other); for callers that do not link the CUDA runtime themselves.  Freed with tcym_host_free. */
+int tcym_host_alloc(size_t bytes, void **ptr);
+int tcym_host_free(void *ptr);
 
 /* ------------------------------------------------------ initial conditions */
 /* InitialConditions::SetZero (INITIALCONDITIONS/SetZero.cpp:3-24): U = 1, E = 0. */

@@ -134,3 +134,29 @@ def test_host_step_pinned_graph_replay(ctx, oracle_port, monkeypatch, nc):
         ref.leapfrog(dt, 1)
         Ur, Er = ref.download()
         assert np.array_equal(Ua, Ur) and np.array_equal(Ea, Er), i
+
+
+def test_pinned_arrays_from_the_library(ctx, oracle_port):
+    """tcym.pinned_empty (tcym_host_alloc): page-locked arrays take the captured-graph
+    pipeline like any pinned memory and are freed with their last view."""
+    import gc
+
+    shape = (16, 16, 12)
+    V = int(np.prod(shape))
+    U0, E0 = state(oracle_port[3], 3, shape, 21)
+    U, E = tcym.pinned_empty((V, 3, 18)), tcym.pinned_empty((V, 3, 8))
+    assert U.flags.c_contiguous and U.flags.writeable and U.dtype == np.float64
+    U[:], E[:] = U0, E0
+    lat = tcym.Lattice(ctx, 3, shape, tcym.FP32)
+    lat.set_reunitarize_period(0)
+    for _ in range(2):
+        lat.leapfrog_host(0.05, U, E, U, E)
+    Us, Es = sequential(ctx, 3, shape, tcym.FP32, U0.copy(), E0.copy(), 0.05, 2)
+    assert np.array_equal(U, Us) and np.array_equal(E, Es)
+    view = U[:10]
+    del U
+    gc.collect()
+    assert np.isfinite(view).all()  # the allocation lives while a view does
+    del view, E
+    gc.collect()
+    assert tcym.pinned_empty((0,)).size == 0

@@ -123,6 +123,8 @@ def library() -> ctypes.CDLL:
         "tcym_lattice_copy": ([ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
         "tcym_lattice_sync": ([ctypes.c_void_p], ctypes.c_int),
         "tcym_lattice_stream": ([ctypes.c_void_p, c_void_pp], ctypes.c_int),
+        "tcym_host_alloc": ([ctypes.c_size_t, c_void_pp], ctypes.c_int),
+        "tcym_host_free": ([ctypes.c_void_p], ctypes.c_int),
         "tcym_set_zero": ([ctypes.c_void_p], ctypes.c_int),
         "tcym_gaussian_efield": ([ctypes.c_void_p, ctypes.c_double, ctypes.c_uint64], ctypes.c_int),
         "tcym_write_configuration": ([ctypes.c_int] * 4 + [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_char_p,
@@ -193,6 +195,34 @@ def _ptr(a):
         return None
     assert a.dtype == np.float64 and a.flags.c_contiguous
     return a.ctypes.data_as(ctypes.c_void_p)
+
+
+class _PinnedBuffer:
+    """Owns page-locked host memory from tcym_host_alloc; freed when the last array viewing it goes."""
+
+    def __init__(self, nbytes: int):
+        self.lib = library()
+        p = ctypes.c_void_p()
+        rc = self.lib.tcym_host_alloc(nbytes, ctypes.byref(p))
+        if rc != 0:
+            raise TcymError(rc, "tcym_host_alloc failed")
+        self.ptr, self.nbytes = p.value, nbytes
+
+    def __del__(self):
+        if getattr(self, "ptr", None):
+            self.lib.tcym_host_free(ctypes.c_void_p(self.ptr))
+            self.ptr = None
+
+
+def pinned_empty(shape, dtype=np.float64) -> np.ndarray:
+    """A C-contiguous array in page-locked host memory (tcym_host_alloc): the host arrays
+    of upload / download / leapfrog_host, whose copies then run asynchronously."""
+    dtype = np.dtype(dtype)
+    n = int(np.prod(shape))
+    buf = _PinnedBuffer(max(1, n * dtype.itemsize))
+    raw = (ctypes.c_char * buf.nbytes).from_address(buf.ptr)
+    raw._owner = buf  # the ctypes array keeps the allocation alive; numpy keeps the ctypes array
+    return np.frombuffer(raw, dtype=dtype, count=n).reshape(shape)
 
 
 class Context:

@@ -412,6 +412,26 @@ extern "C" int tcym_lattice_stream(tcym_lattice lat, void **stream) {
     return TCYM_OK;
 }
 
+extern "C" int tcym_host_alloc(size_t bytes, void **ptr) {
+    if (!ptr) return TCYM_ERR_ARG;
+    *ptr = nullptr;
+    if (bytes == 0) return TCYM_OK;
+    const cudaError_t e = cudaMallocHost(ptr, bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        *ptr = nullptr;
+        return e == cudaErrorMemoryAllocation ? TCYM_ERR_OOM : TCYM_ERR_CUDA;
+    }
+    return TCYM_OK;
+}
+extern "C" int tcym_host_free(void *ptr) {
+    if (ptr && cudaFreeHost(ptr) != cudaSuccess) {
+        cudaGetLastError();
+        return TCYM_ERR_ARG;
+    }
+    return TCYM_OK;
+}
+
 // ------------------------------------------------------- initial conditions
 extern "C" int tcym_set_zero(tcym_lattice lat) {
     if (!lat) return TCYM_ERR_ARG;
