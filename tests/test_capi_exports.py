@@ -51,3 +51,16 @@ def test_context_fails_cleanly_without_gpu():
     L = ctypes.CDLL(build.build_library())
     h = ctypes.c_void_p()
     assert L.tcym_ctx_create(0, ctypes.byref(h)) != 0
+
+
+def test_python_mirror_binds_the_c_abi():
+    """Every function of include/tcym.h has a ctypes signature in the Python mirror
+    (the no-alloc restore takes device pointers; its callers bind it themselves)."""
+    import topologicalcymsolver_gb300 as tcym
+
+    src = open(os.path.join(ROOT, "topologicalcymsolver_gb300", "__init__.py")).read()
+    bound = set(re.findall(r'"(tcym_\w+)":\s*\(', src))
+    declared = set(declared_functions())
+    assert declared - bound == {"tcym_gauss_restore_noalloc"}, sorted(declared - bound)
+    assert not bound - declared, sorted(bound - declared)
+    assert callable(tcym.pinned_empty)
