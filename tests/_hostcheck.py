@@ -33,6 +33,7 @@ def load():
         L.hc_observables.argtypes = [ctypes.c_int, ip, _vp, _vp, ctypes.c_int, _vp]
         L.hc_gauss_restore.argtypes = [ctypes.c_int, ip, _vp, _vp, ctypes.c_double, ctypes.c_int]
         L.hc_reunitarize.argtypes = [ctypes.c_int, ip, _vp]
+        L.hc_block.argtypes = [ctypes.c_int, ip, _vp, _vp]
         L.hc_init.argtypes = [ctypes.c_int, ip, _vp, _vp, ctypes.c_int, ctypes.c_double, ctypes.c_uint64]
         L.hc_iexp.argtypes = [ctypes.c_int, ctypes.c_double, _vp, _vp]
         L.hc_ilog.argtypes = [ctypes.c_int, ctypes.c_double, _vp, _vp]
@@ -111,6 +112,10 @@ class HostLattice:
 
     def reunitarize(self):
         self.L.hc_reunitarize(self.fmt, self.n, _p(self.U[self.cur]))
+
+    def block_into(self, other):
+        """Block (site_block) of this lattice's links into `other` (half the extents)."""
+        self.L.hc_block(self.fmt, self.n, _p(self.U[self.cur]), _p(other.U[other.cur]))
 
     def init(self, what, sigma=0.0, seed=0):
         self.L.hc_init(self.fmt, self.n, _p(self.U[self.cur]), _p(self.E), what, sigma, seed)

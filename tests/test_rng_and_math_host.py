@@ -263,3 +263,19 @@ def test_pair_step_tilings(oracle_port, nc):
         assert np.array_equal(Uh, out[0][0]) and np.array_equal(Eh, out[0][1])
     P.leapfrog(shape, U, E, 0.05, 3)
     assert rel(out[0][0], U) < 1e-5 and rel(out[0][1], E) < 1e-5
+
+
+@pytest.mark.parametrize("nc,prec", FORMATS)
+def test_block_matches_oracle(oracle_port, nc, prec):
+    """The device's Block (site_block: U_mu(2x) U_mu(2x + mu) in FP64) on the host, on
+    the stored links, against the oracle's."""
+    P = oracle_port[nc]
+    shape = (4, 6, 8)
+    U, E = _state(P, nc, shape, 23)
+    H = hc.HostLattice(nc, prec, shape)
+    H.upload(U, E)
+    Us, _ = H.download()  # the stored (for FP32: rounded) links
+    B = hc.HostLattice(nc, prec, (2, 3, 4))
+    H.block_into(B)
+    Ub, _ = B.download()
+    assert np.abs(Ub - P.block(shape, Us)).max() < (1e-14 if prec == "f64" else 3e-7)

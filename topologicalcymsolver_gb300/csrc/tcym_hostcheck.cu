@@ -215,6 +215,14 @@ int hc_reunitarize(int fmt, const int *n, void *U) {
     HC_DISPATCH(fmt, for (int64_t s = 0; s < g.V; ++s) site_reunitarize<HH::F>(g, U, s));
     return 0;
 }
+// Block of the links of extents n into Ub (extents n / 2, the same format)
+int hc_block(int fmt, const int *n, const void *U, void *Ub) {
+    const Geom gs = geom(n);
+    const int h[3] = {n[0] / 2, n[1] / 2, n[2] / 2};
+    const Geom gd = geom(h);
+    HC_DISPATCH(fmt, for (int64_t s = 0; s < gd.V; ++s) site_block<HH::F>(gs, gd, U, Ub, s));
+    return 0;
+}
 int hc_init(int fmt, const int *n, void *U, void *E, int what, double sigma, uint64_t seed) {
     Geom g = geom(n);
     HC_DISPATCH(fmt, for (int64_t s = 0; s < g.V; ++s) {
