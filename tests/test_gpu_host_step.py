@@ -160,3 +160,25 @@ def test_pinned_arrays_from_the_library(ctx, oracle_port):
     del view, E
     gc.collect()
     assert tcym.pinned_empty((0,)).size == 0
+
+
+@pytest.mark.parametrize("pinned", [False, True])
+def test_host_step_two_copies_beyond_the_largest_pitch(ctx, oracle_port, monkeypatch, pinned):
+    """Lattices whose half-state rows exceed the device's largest copy pitch (beyond
+    ~200^3) move each chunk's two halves as two copies: forced here with a tiny limit."""
+    monkeypatch.setenv("TCYM_HOST_STEP_MAX_PITCH", "4096")
+    monkeypatch.setenv("TCYM_HOST_STEP_CHUNK", "128")
+    shape = (16, 16, 8)
+    V = int(np.prod(shape))
+    U0, E0 = state(oracle_port[3], 3, shape, 25)
+    if pinned:
+        U, E = tcym.pinned_empty((V, 3, 18)), tcym.pinned_empty((V, 3, 8))
+        U[:], E[:] = U0, E0
+    else:
+        U, E = U0.copy(), E0.copy()
+    lat = tcym.Lattice(ctx, 3, shape, tcym.FP32)
+    lat.set_reunitarize_period(0)
+    for _ in range(2):
+        lat.leapfrog_host(0.05, U, E, U, E)
+    Us, Es = sequential(ctx, 3, shape, tcym.FP32, U0.copy(), E0.copy(), 0.05, 2)
+    assert np.array_equal(U, Us) and np.array_equal(E, Es)

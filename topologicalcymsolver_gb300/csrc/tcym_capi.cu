@@ -121,7 +121,10 @@ extern "C" int tcym_ctx_create(int device, tcym_ctx *out) {
     ctx->device = device;
     if (cudaSetDevice(device) != cudaSuccess) { delete ctx; return TCYM_ERR_CUDA; }
     cudaDeviceProp prop;
-    if (cudaGetDeviceProperties(&prop, device) == cudaSuccess) ctx->sm_count = prop.multiProcessorCount;
+    if (cudaGetDeviceProperties(&prop, device) == cudaSuccess) {
+        ctx->sm_count = prop.multiProcessorCount;
+        ctx->mem_pitch = prop.memPitch;
+    }
     *out = ctx;
     return TCYM_OK;
 }
@@ -619,8 +622,8 @@ extern "C" int tcym_leapfrog(tcym_lattice lat, double dt, int nsteps) {
 // may be U_in).  Each event is waited on right after it is recorded, so one
 // event per edge of the chain suffices.
 template <int FMT>
-static cudaError_t host_step_pipeline(tcym_lattice lat, const StepCoef<double> &c, int64_t C, const double *U_in,
-                                      const double *E_in, double *U_out, double *E_out) {
+static cudaError_t host_step_pipeline(tcym_lattice lat, const StepCoef<double> &c, int64_t C, size_t max_pitch,
+                                      const double *U_in, const double *E_in, double *U_out, double *E_out) {
     using L = Launch<FMT>;
     const int nmd = lat->nc == 2 ? 4 : 18, na = lat->nc == 2 ? 3 : 8;
     const Geom &g = lat->g;
@@ -636,14 +639,20 @@ static cudaError_t host_step_pipeline(tcym_lattice lat, const StepCoef<double> &
     for (cudaStream_t st : lat->hs)
         if (err == cudaSuccess) err = cudaStreamWaitEvent(st, ev[0], 0);
     // both halves of a chunk in one two-row copy (pitch Vh sites), or one range
+    // copies wider than max_pitch (the device's: about 2 GB, lattices beyond ~200^3) take two
     auto copy = [&](double *dst, const double *src, int64_t a, int64_t n, int nd, cudaMemcpyKind kind,
                     cudaStream_t st) {
         if (err != cudaSuccess) return;
         const size_t w = sizeof(double) * 3 * nd * n, pitch = sizeof(double) * 3 * nd * Vh;
-        if (paired)
-            err = cudaMemcpy2DAsync(dst + 3 * nd * a, pitch, src + 3 * nd * a, pitch, w, 2, kind, st);
-        else
-            err = cudaMemcpyAsync(dst + 3 * nd * a, src + 3 * nd * a, w, kind, st);
+        const int64_t off = 3 * nd * a, half = 3 * nd * Vh;
+        if (!paired) {
+            err = cudaMemcpyAsync(dst + off, src + off, w, kind, st);
+        } else if (pitch <= max_pitch) {
+            err = cudaMemcpy2DAsync(dst + off, pitch, src + off, pitch, w, 2, kind, st);
+        } else {
+            err = cudaMemcpyAsync(dst + off, src + off, w, kind, st);
+            if (err == cudaSuccess) err = cudaMemcpyAsync(dst + off + half, src + off + half, w, kind, st);
+        }
     };
     auto link = [&](cudaEvent_t e, cudaStream_t from, cudaStream_t to) {
         if (err == cudaSuccess) err = cudaEventRecord(e, from);
@@ -692,6 +701,16 @@ static int64_t host_step_chunk(tcym_lattice lat, bool paired) {
     }
     return C < 128 ? 128 : C;
 }
+// the largest pitch of the pipeline's two-row copies: the device's, or less
+// (TCYM_HOST_STEP_MAX_PITCH, bytes) so that tests reach the two-copy path
+static size_t host_step_max_pitch(tcym_lattice lat) {
+    size_t p = lat->ctx->mem_pitch;
+    if (const char *env = getenv("TCYM_HOST_STEP_MAX_PITCH")) {
+        const long long v = atoll(env);
+        if (v > 0 && (size_t)v < p) p = (size_t)v;
+    }
+    return p;
+}
 static bool pinned_host(const void *p) {
     cudaPointerAttributes a;
     if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
@@ -731,21 +750,22 @@ extern "C" int tcym_leapfrog_host(tcym_lattice lat, double dt, const double *U_i
     bool paired = false;
     DISPATCH(lat->fmt, paired = L::paired_step(lat->g));
     const int64_t C = host_step_chunk(lat, paired);
+    const size_t max_pitch = host_step_max_pitch(lat);
     const StepCoef<double> c = tcym_coef(lat->a, MODE_LEAPFROG, dt, 0, 0, 0, 0);
     const void *io[4] = {U_in, E_in, U_out, E_out};
     const bool graph = pinned_host(U_in) && pinned_host(E_in) && pinned_host(U_out) && pinned_host(E_out);
     if (!graph) {
-        DISPATCH(lat->fmt, CK(host_step_pipeline<L::FMT_ID>(lat, c, C, U_in, E_in, U_out, E_out)));
+        DISPATCH(lat->fmt, CK(host_step_pipeline<L::FMT_ID>(lat, c, C, max_pitch, U_in, E_in, U_out, E_out)));
     } else {
         auto &h = lat->host_graph[lat->cur];
-        if (!h.exec || h.dt != dt || h.chunk != C || h.staging != lat->staging ||
+        if (!h.exec || h.dt != dt || h.chunk != C || h.max_pitch != max_pitch || h.staging != lat->staging ||
             memcmp(h.io, io, sizeof io) != 0) {
             if (h.exec) cudaGraphExecDestroy(h.exec);
             h = tcym_lattice_s::HostStepGraph{};
             cudaGraph_t gr = nullptr;
             CK(cudaStreamBeginCapture(lat->stream, cudaStreamCaptureModeThreadLocal));
             cudaError_t e = cudaSuccess;
-            DISPATCH(lat->fmt, e = host_step_pipeline<L::FMT_ID>(lat, c, C, U_in, E_in, U_out, E_out));
+            DISPATCH(lat->fmt, e = host_step_pipeline<L::FMT_ID>(lat, c, C, max_pitch, U_in, E_in, U_out, E_out));
             const cudaError_t e2 = cudaStreamEndCapture(lat->stream, &gr);
             if (e == cudaSuccess) e = e2;
             if (e == cudaSuccess) e = cudaGraphInstantiate(&h.exec, gr, 0);
@@ -757,6 +777,7 @@ extern "C" int tcym_leapfrog_host(tcym_lattice lat, double dt, const double *U_i
             memcpy(h.io, io, sizeof io);
             h.dt = dt;
             h.chunk = C;
+            h.max_pitch = max_pitch;
             h.staging = lat->staging;
         }
         CK(cudaGraphLaunch(h.exec, lat->stream));

@@ -14,6 +14,7 @@
 struct tcym_ctx_s {
     int device = 0;
     int sm_count = 152;
+    size_t mem_pitch = (size_t)1 << 31;  // largest pitch of a 2D copy (cudaDeviceProp::memPitch)
     std::mutex mu;
     std::string last_error;
     std::mutex tune_mu;
@@ -56,6 +57,7 @@ struct tcym_lattice_s {
         const void *io[4] = {nullptr, nullptr, nullptr, nullptr};
         double dt = 0;
         int64_t chunk = 0;
+        size_t max_pitch = 0;
         const void *staging = nullptr;
     } host_graph[2];
 };
