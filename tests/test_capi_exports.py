@@ -64,3 +64,22 @@ def test_python_mirror_binds_the_c_abi():
     assert declared - bound == {"tcym_gauss_restore_noalloc"}, sorted(declared - bound)
     assert not bound - declared, sorted(bound - declared)
     assert callable(tcym.pinned_empty)
+
+
+def test_host_alloc_fails_cleanly_without_gpu():
+    """tcym_host_alloc reports an error code (no abort) where the driver has no device;
+    tcym_host_free(NULL) is a no-op."""
+    try:
+        import torch
+        if torch.cuda.is_available():
+            pytest.skip("a GPU is present")
+    except ImportError:
+        pass
+    L = ctypes.CDLL(build.build_library())
+    p = ctypes.c_void_p(1)
+    L.tcym_host_alloc.argtypes = [ctypes.c_size_t, ctypes.POINTER(ctypes.c_void_p)]
+    assert L.tcym_host_alloc(1 << 20, ctypes.byref(p)) != 0
+    assert not p.value
+    assert L.tcym_host_alloc(0, ctypes.byref(p)) == 0 and not p.value
+    L.tcym_host_free.argtypes = [ctypes.c_void_p]
+    assert L.tcym_host_free(None) == 0
