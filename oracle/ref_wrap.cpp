@@ -14,8 +14,15 @@
  *   - GSL: namespace RandomNumberGenerator is supplied here, drawing Philox
  *     normals (orc_philox.h) so that the noise is the same stream the CUDA
  *     kernels draw (MISC/RNG/GSLRandomNumberGenerator.cpp is not included).
- *   - LAPACK zgeev: a stub that aborts; it is reached only from MatrixILog
- *     (SUNc/SU3/AlgebraOperations.cpp:186-233), which is off this path.
+ *   - LAPACK zgeev (not vendored; reached only from MatrixILog,
+ *     SUNc/SU3/AlgebraOperations.cpp:186-233, through
+ *     SUNc/SU3/util/ComplexEigensystem.cpp:27-55): restated below for what
+ *     that call site asks of it, the eigenvalues and right eigenvectors of a
+ *     3x3 complex matrix that is unitary there (a normal matrix): a cyclic
+ *     complex Jacobi on the Hermitian (A + A^dag)/2 + g (A - A^dag)/2i, which
+ *     shares A's eigenvectors, then lambda_j = v_j^dag A v_j.  MatrixILog's
+ *     result, sum_j v_j (i c arg lambda_j) v_j^dag, does not depend on the
+ *     eigenvectors' order or phases, so any exact eigendecomposition gives it.
  *   - The time steps Dynamics::dTau (DYNAMICS/Dynamics.cpp:17),
  *     LangevinDynamics::dTauL (DYNAMICS/LangevinDynamics.cpp:41) and
  *     ThermalDynamics::dTau (DYNAMICS/ThermalDynamics.cpp:23) are declared
@@ -65,10 +72,70 @@ namespace RandomNumberGenerator {
 }
 
 #if SU_Nc_FLAG == SU3_FLAG
-extern "C" void zgeev(char const *, char const *, int *, COMPLEX *, int *, COMPLEX *, COMPLEX *, int *,
-                      COMPLEX *, int *, COMPLEX *, int *, double *, int *) {
-    std::fprintf(stderr, "oracle: zgeev (SU(3) matrix log) is off the hot path\n");
-    std::abort();
+// Column-major 3x3 (LAPACK's order, ComplexEigensystem.cpp:15-23): M[i + 3 j].
+static void shim_jacobi_hermitian(COMPLEX H[9], COMPLEX W[9]) {
+    for (int k = 0; k < 9; ++k) W[k] = COMPLEX(k % 4 == 0 ? 1.0 : 0.0, 0.0);
+    for (int sweep = 0; sweep < 60; ++sweep) {
+        double off = 0.0;
+        for (int p = 0; p < 3; ++p)
+            for (int q = p + 1; q < 3; ++q) off += std::norm(H[p + 3 * q]);
+        if (off < 1e-300) break;
+        for (int p = 0; p < 3; ++p)
+            for (int q = p + 1; q < 3; ++q) {
+                const COMPLEX hpq = H[p + 3 * q];
+                const double a = std::abs(hpq);
+                if (a < 1e-300) continue;
+                // G = [[c, -s e^{i phi}], [s e^{-i phi}, c]] on (p, q) zeroes (G^dag H G)_pq
+                const COMPLEX e = hpq / a;
+                const double tau = (H[q + 3 * q].real() - H[p + 3 * p].real()) / (2.0 * a);
+                const double t = (tau >= 0 ? 1.0 : -1.0) / (std::fabs(tau) + std::sqrt(1.0 + tau * tau));
+                const double c = 1.0 / std::sqrt(1.0 + t * t), sn = t * c;
+                // columns: H <- H G, W <- W G
+                for (int i = 0; i < 3; ++i) {
+                    const COMPLEX hp = H[i + 3 * p], hq = H[i + 3 * q];
+                    H[i + 3 * p] = c * hp - sn * std::conj(e) * hq;
+                    H[i + 3 * q] = sn * e * hp + c * hq;
+                    const COMPLEX wp = W[i + 3 * p], wq = W[i + 3 * q];
+                    W[i + 3 * p] = c * wp - sn * std::conj(e) * wq;
+                    W[i + 3 * q] = sn * e * wp + c * wq;
+                }
+                // rows: H <- G^dag H
+                for (int j = 0; j < 3; ++j) {
+                    const COMPLEX hp = H[p + 3 * j], hq = H[q + 3 * j];
+                    H[p + 3 * j] = c * hp - sn * e * hq;
+                    H[q + 3 * j] = sn * std::conj(e) * hp + c * hq;
+                }
+                H[p + 3 * q] = H[q + 3 * p] = COMPLEX(0.0, 0.0);
+            }
+    }
+}
+extern "C" void zgeev(char const *, char const *, int *n, COMPLEX *a, int *lda, COMPLEX *w, COMPLEX *vl, int *ldvl,
+                      COMPLEX *vr, int *ldvr, COMPLEX *work, int *lwork, double *, int *info) {
+    if (*lwork == -1) {  // workspace query
+        work[0] = COMPLEX(1.0, 0.0);
+        *info = 0;
+        return;
+    }
+    if (*n != 3 || *lda != 3 || *ldvl != 3 || *ldvr != 3) {
+        *info = -1;
+        return;
+    }
+    const double g = 0.61803398874989484820;  // separates +theta from -theta
+    COMPLEX H[9], W[9];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+            const COMPLEX x = a[i + 3 * j], y = std::conj(a[j + 3 * i]);
+            H[i + 3 * j] = 0.5 * (x + y) + g * (x - y) / COMPLEX(0.0, 2.0);
+        }
+    shim_jacobi_hermitian(H, W);
+    for (int j = 0; j < 3; ++j) {
+        COMPLEX lam(0.0, 0.0);
+        for (int i = 0; i < 3; ++i)
+            for (int k = 0; k < 3; ++k) lam += std::conj(W[i + 3 * j]) * a[i + 3 * k] * W[k + 3 * j];
+        w[j] = lam;
+        for (int i = 0; i < 3; ++i) vr[i + 3 * j] = vl[i + 3 * j] = W[i + 3 * j];  // normal A: left = right
+    }
+    *info = 0;
 }
 #endif
 

@@ -168,6 +168,30 @@ def cooling():
                         cooled=np.array(cooled), steps=16, sqrt_dctau=np.sqrt(0.02), dt=0.05, every=20)
 
 
+def cooling_su3():
+    """SU(3) CoolingMethod, the reference's own (its matrix log reaching the oracle's zgeev
+    restatement): cumulative cooled ΔN_CS and cooled links, level 0 at 6^3, level 1 at 8^3."""
+    P, R = oracle.Port(3), oracle.Ref(3)
+    out = {"dt": 0.05, "every": 20, "sqrt_dctau": np.sqrt(0.02)}
+    for level, shape, steps, bf in ((0, (6, 6, 6), 16, 8), (1, (8, 8, 8), 12, 2)):
+        U, E = oracle.empty_fields(3, shape)
+        P.random_links(shape, U, 0.4, 7 + level)
+        P.gaussian_efield(shape, E, 0.6, 8 + level)
+        P.gauss_restore(shape, U, E, 1e-14, 10000)
+        R.init(shape)
+        R.set(U, E)
+        R.cooling_init(level, steps, bf, np.sqrt(0.02))
+        R.cooling_start()
+        totals, cooled = [], []
+        for _ in range(3):
+            R.leapfrog(0.05, 20)
+            totals.append(R.cooling_update(1))
+            cooled.append(R.cooling_links(level))
+        out.update({f"U0_{level}": U, f"E0_{level}": E, f"totals{level}": np.array(totals),
+                    f"cooled{level}": np.array(cooled), f"steps{level}": steps, f"bf{level}": bf})
+    np.savez_compressed(os.path.join(HERE, "ref_cooling_su3.npz"), **out)
+
+
 def cooling_blocked():
     """CoolingMethod with lattice blocking (StandardBlockingLevel 1 and 2) on SU(2) 8^3:
     the cooled ΔN_CS totals and cooled (blocked) links of three updates."""
@@ -207,6 +231,7 @@ if __name__ == "__main__":
         thermalize(nc)
     cooling()
     cooling_blocked()
+    cooling_su3()
     for nc in (2, 3):
         configuration(nc)
     for f in sorted(os.listdir(HERE)):

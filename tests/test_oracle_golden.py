@@ -222,3 +222,39 @@ def test_block_is_the_product_of_two_links(oracle_port):
             s1 = s0 + step if mu < 2 or 2 * z + 1 < shape[2] else s0 + step - nx * ny * shape[2]
             ref = mat(U[s0, mu]) @ mat(U[s1, mu])
             assert np.abs(mat(Ub[sb, mu]) - ref).max() < 1e-14
+
+
+@pytest.mark.parametrize("level", [0, 1])
+def test_su3_cooling_equals_reference(oracle_port, level):
+    """SU(3) CoolingMethod (level 0 at 6^3, blocking level 1 at 8^3), the reference's own
+    with LAPACK's zgeev restated (its only use: the eigensystem of a unitary 3x3 in
+    MatrixILog): the oracle's cooled links and cumulative cooled Delta N_CS equal it."""
+    d = load("ref_cooling_su3.npz")
+    P = oracle_port[3]
+    U, E = d[f"U0_{level}"].copy(), d[f"E0_{level}"].copy()
+    shape = {0: (6, 6, 6), 1: (8, 8, 8)}[level]
+    small = tuple(k >> level for k in shape)
+    steps, bf, s = int(d[f"steps{level}"]), int(d[f"bf{level}"]), float(d["sqrt_dctau"])
+    old = P.cool_blocked(shape, U, s, steps, level, bf)
+    total = 0.0
+    for k in range(3):
+        P.leapfrog(shape, U, E, float(d["dt"]), int(d["every"]))
+        new = P.cool_blocked(shape, U, s, steps, level, bf)
+        total += P.cooled_delta_ncs(small, old, new, 1)
+        assert rel(new, d[f"cooled{level}"][k]) < 1e-12
+        assert abs(total - d[f"totals{level}"][k]) < 1e-11, (k, total, d[f"totals{level}"][k])
+        old = new
+
+
+def test_su3_matrix_log_equals_reference(oracle_port):
+    """The reference's SU(3) MatrixILog (zgeev restated) against the oracle's log on
+    elements up to and across the branch cut at angle pi."""
+    if not oracle.ref_available(3):
+        pytest.skip("the reference's sources are compiled only where they are present")
+    R = oracle.Ref(3)
+    P = oracle_port[3]
+    rng = np.random.default_rng(3)
+    for scale in (1e-3, 0.1, 1.0, 3.0):
+        for _ in range(10):
+            V = P.matrix_iexp(1.0, rng.normal(size=8) * scale)
+            assert np.abs(R.matrix_ilog(1.0, V) - P.ilog(1.0, V)).max() < 1e-12
