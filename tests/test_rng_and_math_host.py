@@ -279,3 +279,25 @@ def test_block_matches_oracle(oracle_port, nc, prec):
     H.block_into(B)
     Ub, _ = B.download()
     assert np.abs(Ub - P.block(shape, Us)).max() < (1e-14 if prec == "f64" else 3e-7)
+
+
+@pytest.mark.parametrize("nc,prec", FORMATS)
+def test_parity_bounds_catch_a_planted_error(oracle_port, nc, prec):
+    """The parity bounds are tight enough to see a mistake: the same comparison as
+    test_site_step_leapfrog_langevin_flow, with an error planted in the oracle's run
+    (its time step off by 1e-4, and a Langevin noise seed off by one), fails them."""
+    P = oracle_port[nc]
+    shape = (4, 5, 6)
+    U, E = _state(P, nc, shape, 3)
+    H = hc.HostLattice(nc, prec, shape)
+    H.upload(U, E)
+    H.leapfrog(0.05, 10)
+    Ub, Eb = U.copy(), E.copy()
+    P.leapfrog(shape, Ub, Eb, 0.05 * (1 + 1e-4), 10)
+    Uh, Eh = H.download()
+    assert max(rel(Uh, Ub), rel(Eh, Eb)) > TOL[prec]
+    P.leapfrog(shape, U, E, 0.05, 10)
+    H.langevin(0.02, 1.0, 0.6, 3, 0, 2)
+    P.langevin(shape, U, E, 0.02, 1.0, 0.6, 4, 0, 2)
+    Uh, Eh = H.download()
+    assert max(rel(Uh, U), rel(Eh, E)) > TOL[prec]
