@@ -34,6 +34,8 @@ def load():
         L.hc_gauss_restore.argtypes = [ctypes.c_int, ip, _vp, _vp, ctypes.c_double, ctypes.c_int]
         L.hc_reunitarize.argtypes = [ctypes.c_int, ip, _vp]
         L.hc_block.argtypes = [ctypes.c_int, ip, _vp, _vp]
+        L.hc_from_aos_range.argtypes = [ctypes.c_int, ip, _vp, _vp, _vp, _vp, ctypes.c_int64, ctypes.c_int64]
+        L.hc_step_range.argtypes = [ctypes.c_int, ip, _vp, _vp, _vp, ctypes.c_double, ctypes.c_int64, ctypes.c_int64]
         L.hc_init.argtypes = [ctypes.c_int, ip, _vp, _vp, ctypes.c_int, ctypes.c_double, ctypes.c_uint64]
         L.hc_iexp.argtypes = [ctypes.c_int, ctypes.c_double, _vp, _vp]
         L.hc_ilog.argtypes = [ctypes.c_int, ctypes.c_double, _vp, _vp]
@@ -112,6 +114,21 @@ class HostLattice:
 
     def reunitarize(self):
         self.L.hc_reunitarize(self.fmt, self.n, _p(self.U[self.cur]))
+
+    def poison(self):
+        """Every stored value NaN (so that reading anything not written since shows)."""
+        for a in (*self.U, self.E):
+            if a.dtype.kind == "f":
+                a[...] = np.nan
+            else:
+                a.view(np.float32 if self.fmt in (0, 2) else np.float64)[...] = np.nan
+
+    def from_aos_range(self, U, E, s0, count):
+        self.L.hc_from_aos_range(self.fmt, self.n, _p(U), _p(E), _p(self.U[self.cur]), _p(self.E), s0, count)
+
+    def step_range(self, dt, i0, i1):
+        """One leapfrog step of storage indices [i0, i1), new links into the other buffer."""
+        self.L.hc_step_range(self.fmt, self.n, _p(self.U[self.cur]), _p(self.U[1 - self.cur]), _p(self.E), dt, i0, i1)
 
     def block_into(self, other):
         """Block (site_block) of this lattice's links into `other` (half the extents)."""

@@ -72,3 +72,46 @@ def test_schedule_overlaps_steps_with_uploads():
     left = [j for k, j in ops[last_upload + 1:] if k == 1]
     assert sum(b[j + 1] - b[j] for j in left) <= 4 * P  # the last two planes' chunks and the first plane's
     assert last_upload > len(b)  # steps interleave with uploads
+
+
+@pytest.mark.parametrize("nc,prec", [(2, "f32"), (3, "f32"), (3, "f64")])
+@pytest.mark.parametrize("shape", [(8, 8, 12), (8, 8, 9), (16, 16, 8), (6, 10, 14)])
+def test_pipeline_emulated_with_the_device_code(oracle_port, nc, prec, shape):
+    """The library's schedule run with the device's own per-site code (the host check
+    build): storage poisoned with NaN, each chunk converted in from the AoS arrays at its
+    upload, each chunk stepped over its index range (the block offsets of the range
+    launches) at its step; the stepped state equals the whole-lattice step bit for bit
+    and holds no NaN, so no step read a neighbour before its upload."""
+    import numpy as np
+
+    import oracle
+
+    P = oracle_port[nc]
+    U, E = oracle.empty_fields(nc, shape)
+    P.random_links(shape, U, 0.5, 3)
+    P.gaussian_efield(shape, E, 0.7, 4)
+    ref = hc.HostLattice(nc, prec, shape)
+    ref.upload(U, E)
+    ref.step(0, 0.05)  # the whole lattice, linear paired walk (or per site)
+    want = ref.download()
+
+    nx, ny, nz = shape
+    V = nx * ny * nz
+    paired = prec == "f32" and nz % 2 == 0
+    N, Vh = ((V + 1) // 2 if paired else V), (V + 1) // 2
+    H = hc.HostLattice(nc, prec, shape)
+    H.poison()
+    b, ops = hc.pipeline_schedule(N, nx * ny, 128)
+    for kind, j in ops:
+        lo, hi = b[j], b[j + 1]
+        if kind == 0:
+            H.from_aos_range(U, E, lo, hi - lo)
+            if paired:
+                H.from_aos_range(U, E, lo + Vh, hi - lo)
+        else:
+            H.step_range(0.05, lo, hi)
+    H.cur ^= 1
+    got = H.download()
+    for g_, w_ in zip(got, want):
+        assert not np.isnan(g_).any()
+        assert np.array_equal(g_, w_)

@@ -73,6 +73,27 @@ template <int FMT> struct H {
             else site_step<F, false, true>(g, Uin, Uout, E, c, s);
         }
     }
+    // one fused step of the storage indices [i0, i1) as Launch::step_range runs it: the
+    // paired step's linear blocks from block i0 / 128 (Tile::b0), or sites
+    static void step_range(const Geom &g, const void *Uin, void *Uout, void *E, const StepCoef<double> &cd,
+                           int64_t i0, int64_t i1) {
+        StepCoef<T> c = cast<T>(cd);
+        if constexpr (F::PAIRED) {
+            if (g.nz % 2 == 0) {
+                const Tile t{0, 0, 0, 0, 0, (int)(i0 / 128)};
+                for (int64_t b = 0; b < (i1 - i0 + 127) / 128; ++b)
+                    for (int tid = 0; tid < 128; ++tid) {
+                        int64_t p;
+                        bool seam;
+                        if (!tile_pair(g, t, b, tid, p, seam)) continue;
+                        if (seam) site_step_pair<F, true>(g, Uin, Uout, E, c, p);
+                        else site_step_pair<F, false>(g, Uin, Uout, E, c, p);
+                    }
+                return;
+            }
+        }
+        for (int64_t s = i0; s < i1; ++s) site_step<F, true, true>(g, Uin, Uout, E, c, s);
+    }
     static void flow_cb(const Geom &g, void *U, double dtau, int nsweeps) {
         const T fc[3] = {T(-2), T(-2), T(-2)}, cn[3] = {T(1), T(1), T(1)}, uc[3] = {T(-dtau), T(-dtau), T(-dtau)};
         for (int sw = 0; sw < nsweeps; ++sw)
@@ -178,6 +199,20 @@ extern "C" {
 int hc_from_aos(int fmt, const int *n, const double *Ua, const double *Ea, void *U, void *E) {
     Geom g = geom(n);
     HC_DISPATCH(fmt, for (int64_t s = 0; s < g.V; ++s) site_from_aos<HH::F>(g, U, E, Ua, Ea, s));
+    return 0;
+}
+// sites [s0, s0 + cnt) of full AoS arrays into the storage
+int hc_from_aos_range(int fmt, const int *n, const double *Ua, const double *Ea, void *U, void *E, int64_t s0,
+                      int64_t cnt) {
+    Geom g = geom(n);
+    HC_DISPATCH(fmt, for (int64_t s = s0; s < s0 + cnt; ++s) site_from_aos<HH::F>(g, U, E, Ua, Ea, s));
+    return 0;
+}
+// one leapfrog step of the storage indices [i0, i1) (site pairs when the format pairs and nz is even)
+int hc_step_range(int fmt, const int *n, const void *Uin, void *Uout, void *E, double dt, int64_t i0, int64_t i1) {
+    Geom g = geom(n);
+    StepCoef<double> c = coef(MODE_LEAPFROG, dt, 0, 0, 0, 0);
+    HC_DISPATCH(fmt, HH::step_range(g, Uin, Uout, E, c, i0, i1));
     return 0;
 }
 int hc_to_aos(int fmt, const int *n, const void *U, const void *E, double *Ua, double *Ea) {
