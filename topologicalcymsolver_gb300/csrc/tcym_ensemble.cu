@@ -197,13 +197,17 @@ template <int FMT> static cudaError_t launch_group_step(tcym_ensemble ens, int f
     using T = typename Fmt<FMT>::T;
     const FmtGroup &G = ens->groups[f];
     const Member<T> *table = static_cast<const Member<T> *>(G.d_members);
-    if (!Fmt<FMT>::PAIRED || G.general)
-        return LaunchBatch<FMT>::step(table, (int)G.idx.size(), G.total_blocks, k, G.grid, G.general, s);
-    for (const FmtGroup::Class &c : G.classes) {
-        const cudaError_t e = LaunchBatch<FMT>::step_uniform(table, c.m0, c.m1 - c.m0, c.item0, c.item1, k, c.coef, s);
-        if (e != cudaSuccess) return e;
+    if constexpr (Fmt<FMT>::PAIRED) {
+        if (!G.general) {
+            for (const FmtGroup::Class &c : G.classes) {
+                const cudaError_t e =
+                    LaunchBatch<FMT>::step_uniform(table, c.m0, c.m1 - c.m0, c.item0, c.item1, k, c.coef, s);
+                if (e != cudaSuccess) return e;
+            }
+            return cudaSuccess;
+        }
     }
-    return cudaSuccess;
+    return LaunchBatch<FMT>::step(table, (int)G.idx.size(), G.total_blocks, k, G.grid, G.general, s);
 }
 
 static cudaError_t group_step(tcym_ensemble ens, int f, int k, cudaStream_t s) {
