@@ -276,6 +276,7 @@ static cudaError_t join_side(tcym_lattice lat) {
 }
 
 extern "C" int tcym_lattice_upload(tcym_lattice lat, const double *U_aos, const double *E_aos) {
+    TCYM_RANGE("tcym_lattice_upload");
     if (!lat) return TCYM_ERR_ARG;
     tcym_ctx ctx = lat->ctx;
     cudaSetDevice(ctx->device);
@@ -307,6 +308,7 @@ extern "C" int tcym_lattice_upload(tcym_lattice lat, const double *U_aos, const 
 }
 
 extern "C" int tcym_lattice_download(tcym_lattice lat, double *U_aos, double *E_aos) {
+    TCYM_RANGE("tcym_lattice_download");
     if (!lat) return TCYM_ERR_ARG;
     tcym_ctx ctx = lat->ctx;
     cudaSetDevice(ctx->device);
@@ -480,6 +482,7 @@ static int fetch_result(tcym_lattice lat) {
 }
 
 extern "C" int tcym_gauss_restore(tcym_lattice lat, double tol, int maxit, int *iters, double *final_max) {
+    TCYM_RANGE("tcym_gauss_restore");
     if (!lat || maxit < 0) return TCYM_ERR_ARG;
     tcym_ctx ctx = lat->ctx;
     cudaSetDevice(ctx->device);
@@ -528,6 +531,7 @@ extern "C" int tcym_gauss_restore(tcym_lattice lat, double tol, int maxit, int *
 // TYY, TZZ, ELECTRIC, MAGNETIC (BulkObservables.cpp:29-52).
 extern "C" int tcym_thermalize(tcym_lattice lat, double beta, uint64_t seed, int rounds, double max_time, double dt,
                                double restore_tol, int every, double *series, int series_cap, int *records) {
+    TCYM_RANGE("tcym_thermalize");
     if (!lat || !(beta > 0) || rounds < 0 || !(dt > 0) || every < 0 || series_cap < 0 ||
         (series_cap > 0 && !series))
         return TCYM_ERR_ARG;
@@ -587,6 +591,7 @@ static int maybe_reunitarize(tcym_lattice lat) {
 
 int tcym_run_steps(tcym_lattice lat, int mode, double dt, double gamma, double T, uint64_t seed, uint64_t step0,
                    int nsteps) {
+    TCYM_RANGE("tcym_steps");
     tcym_ctx ctx = lat->ctx;
     cudaSetDevice(ctx->device);
     for (int i = 0; i < nsteps; ++i) {
@@ -732,6 +737,7 @@ static bool pinned_host(const void *p) {
 // of host-issued operations whose issue order would tie the two directions.
 extern "C" int tcym_leapfrog_host(tcym_lattice lat, double dt, const double *U_in, const double *E_in,
                                   double *U_out, double *E_out) {
+    TCYM_RANGE("tcym_leapfrog_host");
     if (!lat || !U_in || !E_in || !U_out || !E_out) return TCYM_ERR_ARG;
     tcym_ctx ctx = lat->ctx;
     cudaSetDevice(ctx->device);
@@ -815,6 +821,7 @@ extern "C" int tcym_update_u(tcym_lattice lat, double dt) {
 }
 
 extern "C" int tcym_flow(tcym_lattice lat, double dtau, int nsteps, int mode, int calibrate, double *dncs) {
+    TCYM_RANGE("tcym_flow");
     if (!lat || nsteps < 0 || (mode != TCYM_FLOW_SIMULTANEOUS && mode != TCYM_FLOW_CHECKERBOARD) || calibrate < 0 ||
         calibrate > 2)
         return TCYM_ERR_ARG;
@@ -881,6 +888,7 @@ extern "C" int tcym_set_reunitarize_period(tcym_lattice lat, int period) {
 
 // ---------------------------------------------------------------- observables
 extern "C" int tcym_observables(tcym_lattice lat, tcym_obs *out) {
+    TCYM_RANGE("tcym_observables");
     if (!lat || !out) return TCYM_ERR_ARG;
     cudaSetDevice(lat->ctx->device);
     int r = tcym_reduce(lat, OBS_ALL, 0.0);

@@ -213,6 +213,7 @@ extern "C" int tcym_cooling_start(tcym_cooling c) {
 
 // CoolingMethod::Update(Measure) (:141-166)
 extern "C" int tcym_cooling_update(tcym_cooling c, int measure, double *delta) {
+    TCYM_RANGE("tcym_cooling_update");
     if (!c) return TCYM_ERR_ARG;
     if (!c->started) {
         tcym_set_error(c->hot->ctx, "tcym_cooling_update: call tcym_cooling_start first");

@@ -326,6 +326,7 @@ extern "C" int tcym_ensemble_size(tcym_ensemble ens, int *n) {
 }
 
 extern "C" int tcym_ensemble_step(tcym_ensemble ens, int nsteps) {
+    TCYM_RANGE("tcym_ensemble_step");
     if (!ens || nsteps < 0) return TCYM_ERR_ARG;
     if (nsteps == 0 || ens->members.empty()) return TCYM_OK;
     cudaSetDevice(ens->ctx->device);

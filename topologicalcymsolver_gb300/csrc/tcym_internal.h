@@ -8,8 +8,20 @@
 #include <mutex>
 #include <string>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "../../include/tcym.h"
 #include "tcym_site.cuh"
+
+// An NVTX range over the rest of the scope: the library's entry points show by
+// name on an nsys or ncu timeline (a few nanoseconds when no tool listens).
+struct TcymRange {
+    explicit TcymRange(const char *name) { nvtxRangePushA(name); }
+    ~TcymRange() { nvtxRangePop(); }
+    TcymRange(const TcymRange &) = delete;
+    TcymRange &operator=(const TcymRange &) = delete;
+};
+#define TCYM_RANGE(name) TcymRange tcym_range_scope_(name)
 
 struct tcym_ctx_s {
     int device = 0;
