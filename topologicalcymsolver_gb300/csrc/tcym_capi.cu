@@ -691,11 +691,13 @@ static cudaError_t host_step_pipeline(tcym_lattice lat, const StepCoef<double> &
     return err;
 }
 
-// Units per chunk of the host-step pipeline: about 64 MB of host data, a
-// multiple of 128 (TCYM_HOST_STEP_CHUNK overrides, in units).  Measured on
-// GB300 at 128^3 SU(3): 8.9 ms per step with 64 MB chunks, 9.5-14 ms with
-// 16 MB and 12 ms with 5 MB (more, smaller copies), against 14.3 ms for the
-// three calls upload, step, download.
+// Units per middle chunk of the host-step pipeline (the ends take one z-plane
+// chunks, pipeline_bounds): about 64 MB of host data, a multiple of 128
+// (TCYM_HOST_STEP_CHUNK overrides, in units).  Measured on GB300 at 128^3
+// SU(3) with uniform chunks: 8.9 ms per step with 64 MB, 9.5-14 ms with 16 MB,
+// 12 ms with 5 MB (more, smaller copies), 9.3 ms with 128 MB, against 14.1 ms
+// for the three calls upload, step, download; the one-plane ends then took the
+// 64 MB case to 8.75 ms.
 static int64_t host_step_chunk(tcym_lattice lat, bool paired) {
     const int nmd = lat->nc == 2 ? 4 : 18, na = lat->nc == 2 ? 3 : 8;
     const int64_t unit_bytes = (int64_t)sizeof(double) * 3 * (nmd + na) * (paired ? 2 : 1);
