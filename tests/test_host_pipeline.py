@@ -115,3 +115,26 @@ def test_pipeline_emulated_with_the_device_code(oracle_port, nc, prec, shape):
     for g_, w_ in zip(got, want):
         assert not np.isnan(g_).any()
         assert np.array_equal(g_, w_)
+
+
+def test_schedule_on_random_extents_and_chunks():
+    """300 seeded random lattices (extents 1..20, paired or not) and chunk sizes."""
+    import numpy as np
+
+    rng = np.random.default_rng(11)
+    for _ in range(300):
+        nx, ny = int(rng.integers(1, 21)), int(rng.integers(1, 21))
+        nzp = int(rng.integers(1, 13))
+        C = 128 * int(rng.integers(1, 9))
+        check_schedule(nx, ny, nzp, C)
+
+
+def test_pipeline_emulated_on_random_shapes(oracle_port):
+    """Eight seeded random shapes through the poisoned emulation (SU(2) FP32 and FP64)."""
+    import numpy as np
+
+    rng = np.random.default_rng(12)
+    for k in range(8):
+        shape = tuple(int(x) for x in rng.integers(3, 13, size=3))
+        prec = "f32" if k % 2 == 0 else "f64"
+        test_pipeline_emulated_with_the_device_code(oracle_port, 2, prec, shape)
