@@ -12,7 +12,7 @@ CUDA library draws); every output below is produced by the reference itself:
                            gradient flow 10 steps (dtau 0.02, CalibrationUpdate),
                            Gauss restore, and the observables of each state
   ref_group_su{2,3}.npz    MatrixIExp, ReTrIGenU, (Inverse)AdjointMultiplication
-  ref_c0_su2_16.npz        BASELINE config 0: SU(2) 16^3, U = 1, E ~ N(0, 1/2)
+  ref_leapfrog_su2_16.npz  SU(2) 16^3 leapfrog series: U = 1, E ~ N(0, 1/2)
                            (seed 1) Gauss-restored by the reference, 1000 leapfrog
                            steps at dt 0.05, observables every 10 steps
   ref_thermalize_su{2,3}.npz  ThermalDynamics::Thermalize(2, 0.75) on a (4,4,6)
@@ -103,7 +103,7 @@ def group(nc):
                         adj=adj, iadj=iadj)
 
 
-def config0():
+def leapfrog_series_su2_16():
     R = oracle.Ref(2)
     shape = (16, 16, 16)
     R.init(shape)
@@ -114,7 +114,7 @@ def config0():
     for _ in range(100):
         R.leapfrog(0.05, 10)
         series.append(R.observables())
-    np.savez_compressed(os.path.join(HERE, "ref_c0_su2_16.npz"), E_ic=E, series=np.array(series), dt=0.05,
+    np.savez_compressed(os.path.join(HERE, "ref_leapfrog_su2_16.npz"), E_ic=E, series=np.array(series), dt=0.05,
                         every=10)
 
 
@@ -226,7 +226,7 @@ if __name__ == "__main__":
     for nc in (2, 3):
         states(nc)
         group(nc)
-    config0()
+    leapfrog_series_su2_16()
     for nc in (2, 3):
         thermalize(nc)
     cooling()

@@ -2,8 +2,8 @@
 
 * Per observable (T00, E^2, B^2, Gauss max/rms, unitarity max, clover and improved
   E.B, Kahan N_CS), the relative error of the FP64 and FP32 device paths against
-  the oracle over the first 100 steps of the config-0 start (SU(2) 16^3 leapfrog)
-  and of the config-1 start (SU(3) Langevin, 32^3 here); the table is printed
+  the oracle over the first 100 steps of an SU(2) 16^3 leapfrog start and of an
+  SU(3) Langevin start (32^3 here); the table is printed
   (pytest -s) and bounded: FP64 1e-10, FP32 1e-5 (E.B and N_CS: relative to the
   mean |E.B|, since they are sums that cancel).
 * N_CS diffusion: 24 thermal SU(2) 12^3 trajectories stepped 2000 steps in an
@@ -37,9 +37,9 @@ NAMES = ["T00", "E^2/2", "B^2/2", "Gauss |max|", "Gauss rms", "unitarity max", "
 
 
 @pytest.mark.parametrize("prec", [tcym.FP64, tcym.FP32], ids=["fp64", "fp32"])
-@pytest.mark.parametrize("config", ["c0", "c1"])
-def test_observable_errors(ctx, oracle_port, config, prec):
-    if config == "c0":
+@pytest.mark.parametrize("start", ["su2_leapfrog", "su3_langevin"])
+def test_observable_errors(ctx, oracle_port, start, prec):
+    if start == "su2_leapfrog":
         nc, shape, P = 2, (16, 16, 16), oracle_port[2]
         U, E = oracle.empty_fields(2, shape)
         P.set_zero(shape, U, E)
@@ -76,15 +76,15 @@ def test_observable_errors(ctx, oracle_port, config, prec):
     scale[8] = max(np.abs(ref[:, 6]).mean() * dt * 10 / (8 * np.pi ** 2) * len(ref), 1e-12)
     err = np.abs(got - ref).max(axis=0) / np.maximum(scale, 1e-300)
     tol = 1e-10 if prec == tcym.FP64 else 1e-5
-    print(f"\n{config} {'FP64' if prec == tcym.FP64 else 'FP32'} max relative error over 100 steps:")
+    print(f"\n{start} {'FP64' if prec == tcym.FP64 else 'FP32'} max relative error over 100 steps:")
     for name, e in zip(NAMES, err):
         print(f"  {name:14s} {e:.2e}")
     for i, name in enumerate(NAMES):
-        if name == "unitarity max" or (config == "c0" and name.startswith("Gauss")):
+        if name == "unitarity max" or (start == "su2_leapfrog" and name.startswith("Gauss")):
             # violations of a restored / unitary state are rounding-level absolute numbers
             # (~1e-14 in FP64, ~1e-7 in FP32): bounded absolutely
             assert np.abs(got[:, i]).max() < (1e-10 if prec == tcym.FP64 else 1e-4), name
-        else:  # the Langevin noise breaks Gauss's law (config 1): its violation compares relatively
+        else:  # the Langevin noise breaks Gauss's law (the SU(3) Langevin run): its violation compares relatively
             assert err[i] < tol, (name, err[i])
 
 

@@ -46,7 +46,7 @@ def test_leapfrog_parity(ctx, oracle_port, nc, prec, shape):
             # this rough random start (sigma_U = 0.6) is chaotic enough to amplify the
             # FP32 storage rounding ~6x per 50 steps (1.3e-6 at step 50, 8e-6..1e-5 at
             # 100, the same for the host build of the paired and the per-site step);
-            # the configurations' own starts keep 1e-5 over 100 steps (test_gpu_configs)
+            # the configurations' own starts keep 1e-5 over 100 steps (test_gpu_reference_runs)
             tol = 3e-5
         assert rel(Ug, U) < tol, (total, rel(Ug, U))
         assert rel(Eg, E) < tol, (total, rel(Eg, E))

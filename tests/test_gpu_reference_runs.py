@@ -1,14 +1,14 @@
-"""The BASELINE configurations as parity tests (GPU through the C ABI).
+"""The reference runs this path is measured on, as parity tests (GPU through the C ABI).
 
-config 0: SU(2) 16^3, U = 1, E ~ N(0, 1/2) (seed 1) Gauss-restored, 1000 leapfrog
+SU(2) 16^3 leapfrog: U = 1, E ~ N(0, 1/2) (seed 1) Gauss-restored, 1000 leapfrog
   steps at dt 0.05, observables every 10 steps: compared with the reference's own
-  series (tests/golden/ref_c0_su2_16.npz) pointwise over the first 100 steps
+  series (tests/golden/ref_leapfrog_su2_16.npz) pointwise over the first 100 steps
   and, beyond the chaotic horizon, through the conserved energy.
-config 1: SU(3) Langevin 64^3, dt 0.02, gamma 1, T 0.6, links exp(i theta lambda/2)
+SU(3) 64^3 Langevin: dt 0.02, gamma 1, T 0.6, links exp(i theta lambda/2)
   theta ~ N(0, 0.09) (seed 2), E = 0, noise seed 3: pointwise against the FP64
   oracle fed the identical noise for 100 steps (FP64 <= 1e-10, FP32 <= 1e-5
   relative), and the Kahan-integrated N_CS over the first 10.
-config 2: leapfrog, then checkerboarded gradient-flow cooling sweeps at
+SU(2) 96^3 cooling: leapfrog, then checkerboarded gradient-flow cooling sweeps at
   dtau 0.02: at 32^3 against the oracle's checkerboard restatement every 10
   sweeps; at the full 96^3 (2000 leapfrog steps, 500 sweeps) FP32 storage
   against the FP64 path over the first 30 sweeps, and the energy decaying
@@ -35,8 +35,8 @@ def rel(a, b):
 
 # tolerances: (energies, E.B) relative to max(1, |value|)
 @pytest.mark.parametrize("prec,tol_e,tol_edb", [(tcym.FP64, 1e-10, 1e-8), (tcym.FP32, 2e-5, 2e-3)])
-def test_config0_against_reference_series(ctx, prec, tol_e, tol_edb):
-    d = dict(np.load(os.path.join(G, "ref_c0_su2_16.npz")))
+def test_su2_16_leapfrog_against_reference_series(ctx, prec, tol_e, tol_edb):
+    d = dict(np.load(os.path.join(G, "ref_leapfrog_su2_16.npz")))
     s = d["series"]
     shape = (16, 16, 16)
     ic = tcym.Lattice(ctx, 2, shape, tcym.FP64)
@@ -68,7 +68,7 @@ def test_config0_against_reference_series(ctx, prec, tol_e, tol_edb):
 
 
 @pytest.mark.parametrize("prec,tol", [(tcym.FP64, 1e-10), (tcym.FP32, 1e-5)])
-def test_config1_langevin_64_identical_noise(ctx, oracle_port, prec, tol):
+def test_su3_64_langevin_identical_noise(ctx, oracle_port, prec, tol):
     P = oracle_port[3]
     shape = (64, 64, 64)
     U, E = oracle.empty_fields(3, shape)
@@ -107,7 +107,7 @@ def _cooling_input(ctx, shape, nlf, tol=1e-14):
 
 
 @pytest.mark.parametrize("prec,tol", [(tcym.FP64, 1e-10), (tcym.FP32, 2e-5)])
-def test_config2_cooling_against_oracle(ctx, oracle_port, prec, tol):
+def test_su2_cooling_sweeps_against_oracle(ctx, oracle_port, prec, tol):
     P = oracle_port[2]
     shape = (32, 32, 32)
     src = _cooling_input(ctx, shape, 200)
@@ -129,7 +129,7 @@ def test_config2_cooling_against_oracle(ctx, oracle_port, prec, tol):
     assert all(b < a for a, b in zip(mags, mags[1:]))  # cooling lowers the magnetic energy
 
 
-def test_config2_full_size_fp32_tracks_fp64(ctx):
+def test_su2_96_cooling_fp32_tracks_fp64(ctx):
     shape = (96, 96, 96)
     l64 = _cooling_input(ctx, shape, 2000, tol=1e-12)
     l32 = tcym.Lattice(ctx, 2, shape, tcym.FP32)
@@ -173,8 +173,8 @@ def test_energy_drift_fp32_vs_fp64(ctx):
 
 
 @pytest.mark.parametrize("prec,tol", [(tcym.FP64, 1e-9), (tcym.FP32, 1e-4)])
-def test_config2_cooled_ncs_series(ctx, oracle_port, prec, tol):
-    """Config 2's cooled N_CS: Delta N_CS accumulated along the gradient flow as
+def test_su2_cooled_ncs_series(ctx, oracle_port, prec, tol):
+    """The cooling run's cooled N_CS: Delta N_CS accumulated along the gradient flow as
     GradientFlow::CalibrationUpdate does (GradientFlow.cpp:168-188, improved E.B),
     every 10 steps of dtau 0.02, against the oracle (32^3, from the leapfrogged state)."""
     P = oracle_port[2]

@@ -103,11 +103,11 @@ def test_observables_of_inputs(oracle_port, nc):
         assert abs(o[k] - r[k]) < 1e-12 * max(1.0, abs(r[k])), oracle.OBS_FIELDS[k]
 
 
-def test_config0_initial_state_and_series(oracle_port):
-    """BASELINE config 0 (SU(2) 16^3): the oracle's IC equals the reference's, and the
+def test_su2_16_leapfrog_initial_state_and_series(oracle_port):
+    """The SU(2) 16^3 leapfrog run: the oracle's IC equals the reference's, and the
     first 100 steps of the energy series agree pointwise."""
     P = oracle_port[2]
-    d = load("ref_c0_su2_16.npz")
+    d = load("ref_leapfrog_su2_16.npz")
     shape = (16, 16, 16)
     U, E = oracle.empty_fields(2, shape)
     P.set_zero(shape, U, E)
