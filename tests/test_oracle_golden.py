@@ -258,3 +258,7 @@ def test_su3_matrix_log_equals_reference(oracle_port):
         for _ in range(10):
             V = P.matrix_iexp(1.0, rng.normal(size=8) * scale)
             assert np.abs(R.matrix_ilog(1.0, V) - P.ilog(1.0, V)).max() < 1e-12
+    # degenerate eigenvalues: the identity, and exp(i theta t_8) (two equal phases)
+    for al in (np.zeros(8), np.eye(8)[7] * 1.3, np.eye(8)[7] * -2.2 + np.eye(8)[2] * 1e-9):
+        V = P.matrix_iexp(1.0, al)
+        assert np.abs(R.matrix_ilog(1.0, V) - P.ilog(1.0, V)).max() < 1e-9
