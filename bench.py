@@ -51,6 +51,7 @@ def parse():
     p.add_argument("--dt", type=float, default=0.05)
     p.add_argument("--e2e-steps", type=int, default=10)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 path's sub-record")
     # other configurations of the reference's workload, each with its own JSON line:
     # ensemble = 256 mixed trajectories in batched launches; serve = Poisson request stream
     p.add_argument("--workload", default="leapfrog", choices=["leapfrog", "ensemble", "serve"])
@@ -60,15 +61,27 @@ def parse():
 
 
 def config(L, dt):
+    """The workload, identical in both arms (what is computed, not how it is stored)."""
     return {
-        "workload": f"SU(3) Hamiltonian leapfrog {L}^3, dt={dt}, FP32 two-row link storage, FP64 reunitarisation "
-                    f"every 100 steps",
-        "group": "SU(3)", "L": L, "dt": dt, "storage": "fp32 two-row (links 48 B, fields 32 B per link)",
-        "reductions": "fp64", "l2": "inputs larger than L2 (two link buffers + fields, "
-                                    f"{(2 * 48 + 32) * 3 * L ** 3 / 1e6:.0f} MB)",
+        "workload": f"SU(3) Hamiltonian leapfrog {L}^3, dt={dt}",
+        "group": "SU(3)", "L": L, "dt": dt,
+        "l2": "inputs larger than L2 (the 128^3 state is 805 MB in FP32 storage, 1.31 GB in the FP64 AoS layout)",
         "parallelism": "replicas (independent lattices per GPU)",
         "ic": "links exp(i theta t), theta~N(0,0.09) seed 2; E~N(0,0.5) seed 1; FP64 Gauss restore",
     }
+
+
+def impl_config(L, tile):
+    """How our arm stores and steps the workload."""
+    return {"storage": "FP32 two-row SU(3) links (48 B) + FP32 fields (32 B) per link, site pairs packed",
+            "reductions": "fp64", "reunitarisation": "FP64, every 100 steps", "tile": tile,
+            "device": "one GPU"}
+
+
+def reference_impl_config(cores):
+    return {"storage": "FP64 AoS (the reference's GaugeLinks/ElectricFields layout)", "reductions": "fp64",
+            "reunitarisation": "none (the reference never reunitarises)", "tile": "n/a (CPU, OpenMP over z)",
+            "device": f"CPU, {cores} host threads"}
 
 
 # ------------------------------------------------------------------ helpers
@@ -112,15 +125,19 @@ def ncu_traffic():
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    """nvidia-smi clocks, load and throttle reasons, sampled every 200 ms by a
+    read-only query from before the initial-state preparation to the end of the
+    GPU work around the timed region (the timed region alone is a few ms)."""
 
-    Q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
-         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    Q = ("clocks.sm,clocks.max.sm,utilization.gpu,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
 
     def __init__(self, index):
         self.index = index
         self.proc = None
         self.lines = []
+        self.marks = {}
 
     def __enter__(self):
         try:
@@ -135,33 +152,44 @@ class ClockSampler:
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.lines.append((time.monotonic(), line.strip()))
+
+    def mark(self, name):
+        self.marks[name] = time.monotonic()
 
     def __exit__(self, *a):
         if self.proc:
+            time.sleep(0.25)  # one more sample after the last kernel
             self.proc.terminate()
             try:
                 self.proc.wait(timeout=5)
             except Exception:
                 self.proc.kill()
+            self.proc = None
 
     def summary(self):
-        sm, mx, reasons = [], None, set()
+        rows, mx, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        for t, ln in self.lines:
             parts = [p.strip() for p in ln.split(",")]
-            if len(parts) < 6:
+            if len(parts) < 8:
                 continue
             try:
-                sm.append(float(parts[0]))
-                mx = float(parts[1])
+                sm, mx, util = float(parts[0]), float(parts[1]), float(parts[2])
             except ValueError:
                 continue
-            for n, v in zip(names, parts[2:6]):
-                if v.lower().startswith("active"):
-                    reasons.add(n)
-        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
-                "samples": len(sm)}
+            act = {n for n, v in zip(names, parts[4:8]) if v.lower().startswith("active")}
+            rows.append((t, sm, util, act))
+        loaded = [r for r in rows if r[2] >= 50.0]
+        for r in loaded:
+            reasons |= r[3]
+        t0, t1 = self.marks.get("timed_start"), self.marks.get("timed_end")
+        in_timed = [r for r in rows if t0 is not None and t0 - 0.2 <= r[0] <= t1 + 0.2]
+        return {"sm_mhz": statistics.median([r[1] for r in loaded]) if loaded else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(rows), "samples_under_load": len(loaded),
+                "samples_at_timed_region": len(in_timed),
+                "window": "every 200 ms from the initial-state preparation (FP64 restore) through the timed region "
+                          "and the FP64 comparison; under load = utilization.gpu >= 50%"}
 
 
 # --------------------------------------------------------------- CPU timing
@@ -214,6 +242,10 @@ def run_ours(a):
     V = L ** 3
     links = 3 * V
     ctx = tcym.Context(local)
+    # clocks are sampled from the start of the initial-state preparation (seconds of FP64
+    # restore work) through the timed region and the FP64 comparison: the timed region
+    # itself (a few ms) is shorter than the sampling period
+    clk = ClockSampler(local).__enter__()
     # initial state prepared in FP64 (Gauss restore to FP64 precision), then stored in FP32
     ic = tcym.Lattice(ctx, 3, (L, L, L), tcym.FP64)
     ic.random_links(0.3, 2 + 1000 * rank)
@@ -221,7 +253,6 @@ def run_ours(a):
     ic.gauss_restore(1e-12, 400)
     lat = tcym.Lattice(ctx, 3, (L, L, L), tcym.FP32)
     lat.copy_from(ic)
-    ic.close()
     lat.set_reunitarize_period(100)
     stream = torch.cuda.ExternalStream(lat.stream_handle(), device=torch.device("cuda", local))
 
@@ -235,13 +266,14 @@ def run_ours(a):
     if ws > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
-    with ClockSampler(local) as clk:
-        ev[0].record(stream)
-        for k in range(a.steps):
-            lat.leapfrog(dt, 1)
-            ev[k + 1].record(stream)
-        ev[-1].synchronize()
-        torch.cuda.synchronize()
+    clk.mark("timed_start")
+    ev[0].record(stream)
+    for k in range(a.steps):
+        lat.leapfrog(dt, 1)
+        ev[k + 1].record(stream)
+    ev[-1].synchronize()
+    torch.cuda.synchronize()
+    clk.mark("timed_end")
     if ws > 1:
         torch.distributed.barrier()
     per = [ev[k].elapsed_time(ev[k + 1]) * 1e-3 for k in range(a.steps)]
@@ -249,6 +281,30 @@ def run_ours(a):
     reunits = sum(1 for s in range(steps_before + 1, steps_before + a.steps + 1) if s % 100 == 0)
     total = max_over_ranks(total, "cuda")
     value = ws * links * a.steps / total  # the units all ranks processed over the slowest rank's time
+
+    # ---- the plain FP64 path (the compat header's default) on the same start, same K and W
+    fp64 = None
+    if not a.no_fp64:
+        s64 = torch.cuda.ExternalStream(ic.stream_handle(), device=torch.device("cuda", local))
+        for _ in range(a.warmup):
+            ic.leapfrog(dt, 1)
+        ic.sync()
+        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        f0.record(s64)
+        for _ in range(a.steps):
+            ic.leapfrog(dt, 1)
+        f1.record(s64)
+        f1.synchronize()
+        t64 = f0.elapsed_time(f1) * 1e-3 / a.steps
+        fp64 = {"value": links / t64, "unit": UNIT, "ms_per_step": t64 * 1e3, "steps": a.steps,
+                "kernel": "k_step<SU3 FP64> (one site per thread, full 3x3 complex links, FP64 arithmetic)",
+                "bytes_per_link_update": 416,
+                "hbm_frac": round(416 * links / t64 / 1e9 / measured_peak()[0], 4),
+                "fp32_over_fp64": round((total / a.steps) ** -1 / t64 ** -1, 2),
+                "note": "plain FP64 device path (FP64 storage and arithmetic, no reunitarisation), same start, "
+                        "same W and K as the headline; the accuracy of both over 1e4 steps is tested separately"}
+    clk.__exit__()
+    ic.close()
 
     # ---- end to end through the C ABI with pinned host buffers: the state lives in
     # host memory and every step moves it in and out (updated in place, a trajectory)
@@ -296,9 +352,11 @@ def run_ours(a):
     if rank == 0:
         out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": a.steps, "warmup": a.warmup,
                "ms_per_step": total / a.steps * 1e3, "higher_is_better": True, "scaling": "weak",
-               "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": dict(config(L, dt), tile=tile),
-               "e2e": e2e, "roofline": roof, "clocks": clk.summary(), "gpu_launches": a.steps + reunits,
-               "impl": "ours"}
+               "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config(L, dt),
+               "impl_config": impl_config(L, tile), "e2e": e2e, "roofline": roof, "clocks": clk.summary(),
+               "gpu_launches": a.steps + reunits, "impl": "ours"}
+        if fp64 is not None:
+            out["fp64_path"] = fp64
         if ws == 1 and not a.no_cpu_baseline:
             cb = cpu_leapfrog_rate(L, dt, prefer_reference=False)
             out["cpu_baseline"] = cb
@@ -358,6 +416,7 @@ def run_reference(a):
     return {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": a.steps, "warmup": a.warmup,
             "ms_per_step": el / a.steps * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64", "data": "synthetic", "config": config(L, dt), "impl": "reference",
+            "impl_config": reference_impl_config(cores),
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": kind, "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 

@@ -128,6 +128,27 @@ int tcym_lattice_block(const tcym_lattice src, tcym_lattice dst);
 /* dst <- src: links, fields and spacings (same group and extents; any precisions): Copy() of GaugeLinks.cpp:91-107
  * and ElectricFields.cpp:90-104. */
 int tcym_lattice_copy(tcym_lattice dst, const tcym_lattice src);
+/* Binary snapshot of the lattice for an exact resume (no reference counterpart in binary form:
+ * the reference checkpoints only through its 15-digit configuration text files,
+ * IO/SaveConfiguration.cpp:3-56, which tcym_lattice_save writes).  The snapshot holds the links
+ * and fields in the device's own storage format, bit for bit, plus the step count, the
+ * reunitarisation phase, the N_CS tracking period, the Kahan-compensated N_CS pair, the
+ * ping-pong parity and the Langevin noise stream (seed and next step of the last tcym_langevin
+ * call).  Restoring into a lattice of the same group, precision and extents (spacings are taken
+ * from the snapshot) and stepping on gives the same bits as never having stopped.
+ * tcym_lattice_snapshot_bytes: size of the snapshot; tcym_lattice_snapshot: into a host buffer
+ * of at least that size; tcym_lattice_restore: from one (TCYM_ERR_ARG for another lattice's
+ * snapshot, a truncated one or a checksum mismatch).  The _file forms go through a file. */
+int tcym_lattice_snapshot_bytes(tcym_lattice lat, size_t *bytes);
+int tcym_lattice_snapshot(tcym_lattice lat, void *buf, size_t bytes);
+int tcym_lattice_restore(tcym_lattice lat, const void *buf, size_t bytes);
+int tcym_lattice_snapshot_file(tcym_lattice lat, const char *path);
+int tcym_lattice_restore_file(tcym_lattice lat, const char *path);
+/* The Langevin noise stream of the lattice's last tcym_langevin call: its seed and the first step
+ * not yet drawn (valid = 0 before any Langevin step); restored with a snapshot. */
+int tcym_lattice_noise_state(tcym_lattice lat, uint64_t *seed, uint64_t *next_step, int *valid);
+/* Steps taken by the lattice (leapfrog, Langevin, simultaneous flow) since it was created. */
+int tcym_lattice_steps(tcym_lattice lat, int64_t *steps);
 /* Waits for all work queued on the lattice. */
 int tcym_lattice_sync(tcym_lattice lat);
 /* The lattice's CUDA stream (a cudaStream_t), for ordering or timing caller work
@@ -231,16 +252,21 @@ int tcym_gauss_restore(tcym_lattice lat, double tol, int maxit, int *iters, doub
  * U_aos (read) and E_aos (updated) are device pointers on the current device; `stream`
  * is a cudaStream_t (NULL = the default stream); iters / final_max as above (may be
  * NULL); errbuf receives a message on failure (may be NULL).
- * Scratch is a fixed 8 MiB device array inside libtcym.so, held by every GPU that loads
- * the library until the process exits.  Lattices whose violation array (NA * V doubles)
- * exceeds 1,036,272 doubles are rejected with TCYM_ERR_ARG: SU(2) at most 345,424 sites,
- * SU(3) at most 129,534 sites.
- * The first call on a device looks up the scratch address for that device and loads the
- * code of the kernels it runs, for both groups (once; with lazy module loading the runtime
- * would otherwise place each kernel's code in device memory at its first launch); make
- * that first call before any stream capture.  All calls share the one scratch array,
- * which keeps the last call's contents (each call clears what must start at zero): calls
- * that overlap on the GPU, from any thread or stream, race and must not be issued. */
+ * Scratch is a fixed 8 MiB device array inside libtcym.so.  It is reserved on a device
+ * when the library's module that holds it loads there, which with lazy module loading
+ * is the first call of this entry point on that device; that first call also loads the
+ * code of the kernels it runs, for both groups.  Make the first call on each device
+ * before the caller's allocator reserves that device's memory, or it can fail for lack
+ * of memory.  Later calls allocate nothing; the reservation lasts until the process exits.
+ * Lattices whose violation array (NA * V doubles) exceeds 1,036,272 doubles are rejected
+ * with TCYM_ERR_ARG: SU(2) at most 345,424 sites, SU(3) at most 129,534 sites.
+ * Every call reads results back to the host and synchronises `stream` once per
+ * iteration, so no call may run while its stream is being captured into a graph.
+ * All calls share the one scratch array, which keeps the last call's contents (each
+ * call clears what must start at zero): calls that overlap on the GPU, from any thread
+ * or stream, race and must not be issued.
+ * TCYM_ERR_NONFINITE: a reduction saw NaN or Inf in U or E (E is left as it was at that
+ * iteration). */
 int tcym_gauss_restore_noalloc(int nc, int nx, int ny, int nz, const double *U_aos, double *E_aos, double tol,
                                int maxit, void *stream, int *iters, double *final_max, char *errbuf, size_t errlen);
 

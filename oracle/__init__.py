@@ -74,6 +74,8 @@ class Port:
         f("flow").argtypes = [_int_p, _dbl_p, _dbl_p, ctypes.c_double, ctypes.c_int, ctypes.c_int]
         f("flow").restype = ctypes.c_double
         f("flow_checkerboard").argtypes = [_int_p, _dbl_p, ctypes.c_double, ctypes.c_int]
+        f("flow_checkerboard_cal").argtypes = [_int_p, _dbl_p, _dbl_p, ctypes.c_double, ctypes.c_int, ctypes.c_int]
+        f("flow_checkerboard_cal").restype = ctypes.c_double
         f("gauss_restore").argtypes = [_int_p, _dbl_p, _dbl_p, ctypes.c_double, ctypes.c_int]
         f("gauss_restore").restype = ctypes.c_int
         f("observables").argtypes = [_int_p, _dbl_p, _dbl_p, _dbl_p]
@@ -126,6 +128,10 @@ class Port:
 
     def flow_checkerboard(self, shape, U, dtau, nsweeps):
         self._f("flow_checkerboard")(_n(shape), _p(U), dtau, nsweeps)
+
+    def flow_checkerboard_cal(self, shape, U, E, dtau, nsweeps, calibrate=1):
+        """Checkerboard sweeps with the cooled Delta N_CS (trapezoid, improved E.B by default)."""
+        return self._f("flow_checkerboard_cal")(_n(shape), _p(U), _p(E), dtau, nsweeps, calibrate)
 
     def gauss_restore(self, shape, U, E, tol=1e-14, maxit=10000):
         return self._f("gauss_restore")(_n(shape), _p(U), _p(E), tol, maxit)

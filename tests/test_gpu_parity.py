@@ -177,6 +177,26 @@ def test_gauss_restore(ctx, oracle_port, nc):
     assert o[9] <= 1e-13 and o[15] < 1e-12
 
 
+@pytest.mark.parametrize("prec", PREC)
+@pytest.mark.parametrize("nc", GROUPS)
+def test_gauss_restore_reports_nan(ctx, oracle_port, nc, prec):
+    """A NaN in E: the signed maximum drops it (fmax), the sums keep it; the restore
+    must fail with TCYM_ERR_NONFINITE, and a clean restore afterwards must succeed."""
+    shape = (6, 6, 6)
+    P = oracle_port[nc]
+    U, E = random_state(P, nc, shape, seed=53)
+    bad = E.copy()
+    bad[5, 2, 1] = np.nan
+    lat = tcym.Lattice(ctx, nc, shape, prec)
+    lat.upload(U, bad)
+    with pytest.raises(tcym.TcymError) as ei:
+        lat.gauss_restore(1e-14, 10000)
+    assert ei.value.code == 4
+    lat.upload(U, E)
+    lat.gauss_restore(1e-6 if prec == tcym.FP32 else 1e-14, 10000)
+    lat.close()
+
+
 @pytest.mark.parametrize("nc", GROUPS)
 def test_upload_download_roundtrip(ctx, oracle_port, nc):
     shape = (3, 4, 5)

@@ -83,6 +83,26 @@ def test_noalloc_restore_matches_allocating_restore_twice(ctx):
             assert free_after == free_before
 
 
+def test_noalloc_reports_a_nan_in_the_field(ctx):
+    """One NaN in E: the maxima drop it (fmax), the sums do not; the call must
+    return TCYM_ERR_NONFINITE instead of a converged restore."""
+    torch = pytest.importorskip("torch")
+    oracle.build()
+    f = _bind(tcym.library())
+    for nc, shape, seed in ((3, (6, 6, 6), 75), (2, (8, 6, 10), 77)):
+        _, U, E = _input(nc, shape, seed)
+        E[17, 1, 2] = np.nan
+        dev = torch.device("cuda", 0)
+        U_d = torch.from_numpy(U).to(dev)
+        E_d = torch.from_numpy(E).to(dev)
+        torch.cuda.synchronize()
+        stream = torch.cuda.current_stream(dev).cuda_stream
+        rc, it, _, msg = _restore_noalloc(f, nc, shape, U_d.data_ptr(), E_d.data_ptr(), stream)
+        torch.cuda.synchronize()
+        assert rc == 4, (rc, msg)
+        assert it == 0 and "NaN" in msg
+
+
 def test_noalloc_rejects_lattices_beyond_the_scratch(ctx):
     f = _bind(tcym.library())
     # 52^3 SU(3) sites need 8 * 140608 doubles > 1,036,272: rejected before touching the buffers

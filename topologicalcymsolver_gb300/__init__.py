@@ -122,6 +122,14 @@ def library() -> ctypes.CDLL:
                                 ctypes.c_void_p], ctypes.c_int),
         "tcym_lattice_copy": ([ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
         "tcym_lattice_sync": ([ctypes.c_void_p], ctypes.c_int),
+        "tcym_lattice_snapshot_bytes": ([ctypes.c_void_p, ctypes.POINTER(ctypes.c_size_t)], ctypes.c_int),
+        "tcym_lattice_snapshot": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t], ctypes.c_int),
+        "tcym_lattice_restore": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t], ctypes.c_int),
+        "tcym_lattice_snapshot_file": ([ctypes.c_void_p, ctypes.c_char_p], ctypes.c_int),
+        "tcym_lattice_restore_file": ([ctypes.c_void_p, ctypes.c_char_p], ctypes.c_int),
+        "tcym_lattice_noise_state": ([ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64),
+                                      ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
+        "tcym_lattice_steps": ([ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64)], ctypes.c_int),
         "tcym_lattice_stream": ([ctypes.c_void_p, c_void_pp], ctypes.c_int),
         "tcym_host_alloc": ([ctypes.c_size_t, c_void_pp], ctypes.c_int),
         "tcym_host_free": ([ctypes.c_void_p], ctypes.c_int),
@@ -366,6 +374,39 @@ class Lattice:
 
     def random_links(self, sigma: float, seed: int):
         self.ctx.check(self.lib.tcym_random_links(self.h, sigma, seed))
+
+    # ------------------------------------------------------------ snapshots
+    def snapshot(self) -> bytearray:
+        """Binary snapshot of the device state and its counters (tcym_lattice_snapshot)."""
+        n = ctypes.c_size_t()
+        self.ctx.check(self.lib.tcym_lattice_snapshot_bytes(self.h, ctypes.byref(n)))
+        buf = bytearray(n.value)
+        cbuf = (ctypes.c_char * n.value).from_buffer(buf)
+        self.ctx.check(self.lib.tcym_lattice_snapshot(self.h, ctypes.addressof(cbuf), n.value))
+        return buf
+
+    def restore(self, buf) -> None:
+        """State and counters from a snapshot of a lattice with the same group, precision and extents."""
+        b = bytes(buf)
+        self.ctx.check(self.lib.tcym_lattice_restore(self.h, b, len(b)))
+
+    def snapshot_file(self, path) -> None:
+        self.ctx.check(self.lib.tcym_lattice_snapshot_file(self.h, _path(path)))
+
+    def restore_file(self, path) -> None:
+        self.ctx.check(self.lib.tcym_lattice_restore_file(self.h, _path(path)))
+
+    def noise_state(self):
+        """(seed, next noise step, valid) of the last Langevin call."""
+        seed, nxt, ok = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_int()
+        self.ctx.check(self.lib.tcym_lattice_noise_state(self.h, ctypes.byref(seed), ctypes.byref(nxt),
+                                                         ctypes.byref(ok)))
+        return seed.value, nxt.value, bool(ok.value)
+
+    def steps(self) -> int:
+        n = ctypes.c_int64()
+        self.ctx.check(self.lib.tcym_lattice_steps(self.h, ctypes.byref(n)))
+        return n.value
 
     def gauss_restore(self, tol: float = 1e-14, maxit: int = 10000):
         it, mx = ctypes.c_int(), ctypes.c_double()

@@ -26,7 +26,7 @@ NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-rela
 # translation units of libtcym.so (the host-check unit is built separately)
 UNITS = ["tcym_kern_su3_f32.cu", "tcym_kern_su3_f32_batch.cu", "tcym_kern_su3_f64.cu", "tcym_kern_su3_f64_batch.cu",
          "tcym_kern_su2_f32.cu", "tcym_kern_su2_f64.cu", "tcym_reduce.cu", "tcym_capi.cu", "tcym_noalloc.cu",
-         "tcym_ensemble.cu", "tcym_serve.cu", "tcym_cooling.cu", "tcym_io.cu", "tcym_autotune.cu"]
+         "tcym_ensemble.cu", "tcym_serve.cu", "tcym_cooling.cu", "tcym_io.cu", "tcym_autotune.cu", "tcym_snapshot.cu"]
 
 
 def nvcc() -> str:

@@ -497,10 +497,20 @@ extern "C" int tcym_gauss_restore(tcym_lattice lat, double tol, int maxit, int *
         CK(finalize_obs(lat->partial, blocks, na, lat->g.V, 0.0, lat->result, lat->stream));
         return TCYM_OK;
     };
+    // The result block's non-finite flag is sticky; the restore judges only its
+    // own reductions, so it starts from a clear flag.  The signed maximum alone
+    // would miss a NaN (fmax drops it); the flag sees it in the sums.
+    CK(cudaMemsetAsync(lat->result + R_NONFINITE, 0, sizeof(double), lat->stream));
+    auto nonfinite = [&](int at) -> bool {
+        if (lat->host_result[R_NONFINITE] == 0.0 && std::isfinite(lat->host_result[R_GMAX])) return false;
+        tcym_set_error(ctx, "tcym_gauss_restore: non-finite violation at iteration %d", at);
+        return true;
+    };
     // initial deviation (GaussRestore.cpp:143)
     int r = deviation();
     if (r) return r;
     if ((r = fetch_result(lat))) return r;
+    if (nonfinite(0)) return TCYM_ERR_NONFINITE;
     double gmax = lat->host_result[R_GMAX];
     int it = 0;
     while (it < maxit && gmax > tol) {
@@ -511,10 +521,7 @@ extern "C" int tcym_gauss_restore(tcym_lattice lat, double tol, int maxit, int *
         }
         if ((r = fetch_result(lat))) return r;  // max of the last deviation, as the reference tests it
         gmax = lat->host_result[R_GMAX];
-        if (!std::isfinite(gmax)) {
-            tcym_set_error(ctx, "tcym_gauss_restore: non-finite violation at iteration %d", it);
-            return TCYM_ERR_NONFINITE;
-        }
+        if (nonfinite(it)) return TCYM_ERR_NONFINITE;
         ++it;
     }
     if (iters) *iters = it;
@@ -801,7 +808,13 @@ extern "C" int tcym_leapfrog_host(tcym_lattice lat, double dt, const double *U_i
 extern "C" int tcym_langevin(tcym_lattice lat, double dt, double gamma, double T, uint64_t seed, uint64_t step0,
                              int nsteps) {
     if (!lat || nsteps < 0 || gamma < 0 || T < 0 || dt < 0) return TCYM_ERR_ARG;
-    return tcym_run_steps(lat, MODE_LANGEVIN, dt, gamma, T, seed, step0, nsteps);
+    const int r = tcym_run_steps(lat, MODE_LANGEVIN, dt, gamma, T, seed, step0, nsteps);
+    if (r == TCYM_OK) {
+        lat->noise_seed = seed;
+        lat->noise_next = step0 + (uint64_t)nsteps;
+        lat->noise_valid = true;
+    }
+    return r;
 }
 
 extern "C" int tcym_update_e(tcym_lattice lat, double dt) {

@@ -53,6 +53,10 @@ struct tcym_lattice_s {
     int reunit_period = 0, steps_since_reunit = 0;
     int ncs_every = 0;
     int64_t steps_done = 0;
+    // the Langevin noise stream of the last tcym_langevin call: its Philox key and
+    // the first step it has not drawn yet (kept so a snapshot can resume the stream)
+    uint64_t noise_seed = 0, noise_next = 0;
+    bool noise_valid = false;
     tcym::Tile tile{};   // block tiling of the paired step
     bool tile_chosen = false;
     cudaStream_t side[2] = {nullptr, nullptr};  // pipelined host transfers (created with the staging)

@@ -218,6 +218,11 @@ template <class T> struct SU2 {
         out[0] = -w.q[0]; out[1] = -w.q[1]; out[2] = -w.q[2];
     }
     static TCYM_HD void proj(const Mat &v, T *out) { out[0] = -v.q[0]; out[1] = -v.q[1]; out[2] = -v.q[2]; }
+    // proj(a b^dag): only the vector part of the product
+    static TCYM_HD void proj_mul_dag(const Mat &a, const Mat &b, T *out) {
+        const Mat w = mulx<false, true>(a, b);
+        proj(w, out);
+    }
     static TCYM_HD T retr_one_minus(const Mat &v) { return T(2) * (T(1) - v.q[3]); }
     // exp(i c t^k e^k) = cos(d/2) + i sin(d/2) (c e / d).sigma, d = |c e|
     static TCYM_HD Mat iexp(T c, const T *e) {
@@ -374,6 +379,27 @@ template <class T> struct SU3 {
                     cx<T> acc{T(0), T(0)};
 #pragma unroll
                     for (int k = 0; k < 3; ++k) acc = cfma(u.m[i][k], a.m[k][j], acc);
+                    w.m[i][j] = acc;
+                }
+            }
+        proj(w, p);
+    }
+    // proj(a b^dag), W_ij = sum_k a_ik conj(b_jk), computing only the entries proj reads
+    static TCYM_HD void proj_mul_dag(const Mat &a, const Mat &b, T *p) {
+        Mat w;
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                if (i == j) {
+                    T im = T(0);  // Im(a conj(b)) = a.im b.re - a.re b.im
+#pragma unroll
+                    for (int k = 0; k < 3; ++k) im = fma(a.m[i][k].im, b.m[j][k].re, fma(-a.m[i][k].re, b.m[j][k].im, im));
+                    w.m[i][j] = cx<T>{T(0), im};
+                } else {
+                    cx<T> acc{T(0), T(0)};
+#pragma unroll
+                    for (int k = 0; k < 3; ++k) acc = cfma_nc(a.m[i][k], b.m[j][k], acc);
                     w.m[i][j] = acc;
                 }
             }

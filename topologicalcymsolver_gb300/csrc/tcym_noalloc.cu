@@ -19,7 +19,6 @@
 
 #include <cstdio>
 #include <cstring>
-#include <mutex>
 
 #include "../../include/tcym.h"
 #include "tcym_kernels.cuh"
@@ -79,37 +78,31 @@ constexpr size_t kNoAllocViolationCapacity =
 
 static __device__ __align__(256) double g_noalloc_scratch[kNoAllocScratchDoubles];
 
-// Device address of g_noalloc_scratch for each device, looked up once per
-// device with that device current (host code may not use the symbol itself).
-// The same first call loads every kernel the entry point runs, for both groups:
-// with lazy module loading the runtime would otherwise place a kernel's code in
-// device memory at its first launch, i.e. inside a later call.
-static std::mutex g_scratch_mu;
-static double *g_scratch_addr[256];
-
-static cudaError_t scratch_address(int dev, double **out) {
-    std::lock_guard<std::mutex> g(g_scratch_mu);
-    if (dev < 0 || dev >= 256) return cudaErrorInvalidDevice;
-    if (!g_scratch_addr[dev]) {
-        void *p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess) return e;
-        cudaFuncAttributes fa;
-        if ((e = cudaFuncGetAttributes(&fa, k_gauss_compute<FMT_SU2_AOS64>)) != cudaSuccess ||
-            (e = cudaFuncGetAttributes(&fa, k_gauss_compute<FMT_SU3_AOS64>)) != cudaSuccess ||
-            (e = cudaFuncGetAttributes(&fa, k_gauss_update<FMT_SU2_AOS64>)) != cudaSuccess ||
-            (e = cudaFuncGetAttributes(&fa, k_gauss_update<FMT_SU3_AOS64>)) != cudaSuccess ||
-            (e = preload_finalize()) != cudaSuccess)
-            return e;
-        g_scratch_addr[dev] = static_cast<double *>(p);
-    }
-    *out = g_scratch_addr[dev];
+// Device address of g_noalloc_scratch on the current device, looked up on every
+// call with that device current (host code may not use the symbol itself).  The
+// lookup allocates nothing once the module is loaded, and it stays right when
+// the primary context is torn down and created again (the module then reloads
+// and the array may move).  The same call makes sure every kernel the entry
+// point runs is loaded, for both groups: with lazy module loading the runtime
+// would otherwise place a kernel's code in device memory at its first launch.
+static cudaError_t scratch_address(double **out) {
+    void *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return e;
+    cudaFuncAttributes fa;
+    if ((e = cudaFuncGetAttributes(&fa, k_gauss_compute<FMT_SU2_AOS64>)) != cudaSuccess ||
+        (e = cudaFuncGetAttributes(&fa, k_gauss_compute<FMT_SU3_AOS64>)) != cudaSuccess ||
+        (e = cudaFuncGetAttributes(&fa, k_gauss_update<FMT_SU2_AOS64>)) != cudaSuccess ||
+        (e = cudaFuncGetAttributes(&fa, k_gauss_update<FMT_SU3_AOS64>)) != cudaSuccess ||
+        (e = preload_finalize()) != cudaSuccess)
+        return e;
+    *out = static_cast<double *>(p);
     return cudaSuccess;
 }
 
 template <int FMT>
 static cudaError_t restore_aos(const Geom &g, const double *U, double *E, double tol, int maxit, double *scratch,
-                               cudaStream_t st, int *iters, double *final_max) {
+                               cudaStream_t st, int *iters, double *final_max, bool *nonfinite) {
     constexpr int NA = Fmt<FMT>::NA;
     constexpr int TPB = threads_for<FMT>();
     double *result = scratch;
@@ -120,36 +113,41 @@ static cudaError_t restore_aos(const Geom &g, const double *U, double *E, double
     // the array keeps the previous call's contents: clear the result block
     cudaError_t e = cudaMemsetAsync(result, 0, sizeof(double) * R_WIDTH, st);
     if (e != cudaSuccess) return e;
-    auto deviation = [&](double *gmax) -> cudaError_t {
+    // the result block's signed maximum and its non-finite flag (set when a
+    // reduction saw NaN or Inf; the maxima alone would drop a NaN)
+    double host[R_WIDTH];
+    auto fetch = [&](double *gmax, bool *bad) -> cudaError_t {
+        cudaError_t r = cudaMemcpyAsync(host, result, sizeof(host), cudaMemcpyDeviceToHost, st);
+        if (r != cudaSuccess) return r;
+        if ((r = cudaStreamSynchronize(st)) != cudaSuccess) return r;
+        *gmax = host[R_GMAX];
+        *bad = host[R_NONFINITE] != 0.0 || !(host[R_GMAX] == host[R_GMAX]);
+        return cudaSuccess;
+    };
+    auto deviation = [&]() -> cudaError_t {
         k_gauss_compute<FMT><<<blocks, kRedThreads, 0, st>>>(g, U, E, G, partial);
         cudaError_t r = cudaGetLastError();
         if (r != cudaSuccess) return r;
-        if ((r = finalize_obs(partial, blocks, NA, g.V, 0.0, result, st)) != cudaSuccess) return r;
-        if (!gmax) return cudaSuccess;
-        if ((r = cudaMemcpyAsync(gmax, result + R_GMAX, sizeof(double), cudaMemcpyDeviceToHost, st)) != cudaSuccess)
-            return r;
-        return cudaStreamSynchronize(st);
+        return finalize_obs(partial, blocks, NA, g.V, 0.0, result, st);
     };
     const double gam[3] = {7.0 / 24.0, 7.0 / 48.0, 7.0 / 72.0};
     double gmax = 0.0;
-    if ((e = deviation(&gmax)) != cudaSuccess) return e;
+    bool bad = false;
+    if ((e = deviation()) != cudaSuccess || (e = fetch(&gmax, &bad)) != cudaSuccess) return e;
     int it = 0;
-    while (it < maxit && gmax > tol) {
+    while (!bad && it < maxit && gmax > tol) {
         for (int k = 0; k < 3; ++k) {
-            if ((e = deviation(nullptr)) != cudaSuccess) return e;
+            if ((e = deviation()) != cudaSuccess) return e;
             k_gauss_update<FMT><<<grid_for(g.V, TPB), TPB, 0, st>>>(g, U, E, G, gam[k]);
             if ((e = cudaGetLastError()) != cudaSuccess) return e;
         }
         // maximum of the last deviation, as the reference tests it (GaussRestore.cpp:150)
-        if ((e = cudaMemcpyAsync(&gmax, result + R_GMAX, sizeof(double), cudaMemcpyDeviceToHost, st)) != cudaSuccess)
-            return e;
-        if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
+        if ((e = fetch(&gmax, &bad)) != cudaSuccess) return e;
         ++it;
-        if (!(gmax == gmax) || gmax > 1e300) break;  // non-finite: reported by the caller below
     }
-    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
     *iters = it;
     *final_max = gmax;
+    *nonfinite = bad || gmax > 1e300;
     return cudaSuccess;
 }
 
@@ -183,7 +181,7 @@ extern "C" int tcym_gauss_restore_noalloc(int nc, int nx, int ny, int nz, const 
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     double *scratch = nullptr;
-    if (e == cudaSuccess) e = scratch_address(dev, &scratch);
+    if (e == cudaSuccess) e = scratch_address(&scratch);
     if (e != cudaSuccess) {
         char msg[256];
         std::snprintf(msg, sizeof(msg), "tcym_gauss_restore_noalloc: scratch address on device %d: %s", dev,
@@ -193,9 +191,10 @@ extern "C" int tcym_gauss_restore_noalloc(int nc, int nx, int ny, int nz, const 
     const Geom g{nx, ny, nz, V};
     int it = 0;
     double mx = 0.0;
+    bool bad = false;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    e = nc == 2 ? restore_aos<FMT_SU2_AOS64>(g, U_aos, E_aos, tol, maxit, scratch, st, &it, &mx)
-                : restore_aos<FMT_SU3_AOS64>(g, U_aos, E_aos, tol, maxit, scratch, st, &it, &mx);
+    e = nc == 2 ? restore_aos<FMT_SU2_AOS64>(g, U_aos, E_aos, tol, maxit, scratch, st, &it, &mx, &bad)
+                : restore_aos<FMT_SU3_AOS64>(g, U_aos, E_aos, tol, maxit, scratch, st, &it, &mx, &bad);
     if (e != cudaSuccess) {
         char msg[256];
         std::snprintf(msg, sizeof(msg), "tcym_gauss_restore_noalloc: %s", cudaGetErrorString(e));
@@ -203,7 +202,8 @@ extern "C" int tcym_gauss_restore_noalloc(int nc, int nx, int ny, int nz, const 
     }
     if (iters) *iters = it;
     if (final_max) *final_max = mx;
-    if (!(mx == mx) || mx > 1e300)
-        return noalloc_fail(errbuf, errlen, TCYM_ERR_NONFINITE, "tcym_gauss_restore_noalloc: non-finite violation");
+    if (bad)
+        return noalloc_fail(errbuf, errlen, TCYM_ERR_NONFINITE,
+                            "tcym_gauss_restore_noalloc: a reduction saw NaN or Inf (non-finite U or E)");
     return TCYM_OK;
 }

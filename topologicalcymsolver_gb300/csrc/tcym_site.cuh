@@ -153,8 +153,9 @@ TCYM_COLD void langevin_kick_pair(const StepCoef<float> &c, int mu, int64_t p, i
 
 // cn: the Langevin noise's coefficients (seed, step, damping, kick), which may
 // sit apart from the step's (a batched member's own, beside coefficients the
-// members share)
-template <class F, bool SEAM>
+// members share).  MODE >= 0 fixes the step kind at compile time (c.mode is
+// then ignored); -1 reads it from c.
+template <class F, bool SEAM, int MODE = -1>
 TCYM_HD void site_step_pair(const Geom &g, const void *Uin, void *Uout, void *E, const StepCoef<float> &c,
                             const StepCoef<float> &cn, int64_t p, uint64_t step_add) {
     using G2 = typename F::G2;
@@ -180,9 +181,10 @@ TCYM_HD void site_step_pair(const Geom &g, const void *Uin, void *Uout, void *E,
         f2 f[NA];
         G2::proj_mul(u, A, f);
         const f2 fc(sel3(c.fc, mu));
-        if (c.mode == MODE_LANGEVIN) {
+        const int mode = MODE >= 0 ? MODE : c.mode;
+        if (mode == MODE_LANGEVIN) {
             langevin_kick_pair<NA>(cn, mu, p, Vh, step_add, fc, f, e);
-        } else if (c.mode == MODE_FLOW) {
+        } else if (mode == MODE_FLOW) {
 #pragma unroll
             for (int a = 0; a < NA; ++a) e[a] = fc * f[a];
         } else {
@@ -194,10 +196,82 @@ TCYM_HD void site_step_pair(const Geom &g, const void *Uin, void *Uout, void *E,
     }
 }
 
-template <class F, bool SEAM>
+template <class F, bool SEAM, int MODE = -1>
 TCYM_HD void site_step_pair(const Geom &g, const void *Uin, void *Uout, void *E, const StepCoef<float> &c, int64_t p,
                             uint64_t step_add = 0) {
-    site_step_pair<F, SEAM>(g, Uin, Uout, E, c, c, p, step_add);
+    site_step_pair<F, SEAM, MODE>(g, Uin, Uout, E, c, c, p, step_add);
+}
+
+// site_step_pair with the plaquettes shared between directions.  The force on
+// U_mu(x) sums, over nu != mu, the projections of the plaquette above the link
+// (corner x) and of the one below it (corner x - nu); the plaquette above is
+// P_{mu nu}(x) = U_mu(x) S+, and P_{nu mu}(x) = P_{mu nu}(x)^dag, whose
+// projection is the negative.  So the upper staples of all six (mu, nu) come
+// from the three plaquettes P_01, P_12, P_20 at x, each formed once:
+//   f_mu = c_{mu+1} p_{mu,mu+1} - c_{mu+2} p_{mu+2,mu} + proj(U_mu sum_nu c_nu S-_{mu nu})
+// which is the bracket of Dynamics.cpp:184-188 in the staple form above, with 18
+// instead of 24 SU(3) products per site.  The three projections wait in `sm`
+// (this thread's slots, stride `stride`: [plaquette][component]) between the
+// plaquette phase and the per-direction phase.
+template <class F, bool SEAM, int MODE = -1>
+TCYM_HD void site_step_pair_plaq(const Geom &g, const void *Uin, void *Uout, void *E, const StepCoef<float> &c,
+                                 const StepCoef<float> &cn, int64_t p, uint64_t step_add, f2 *sm, int stride) {
+    using G2 = typename F::G2;
+    using M2 = typename F::Mat2;
+    constexpr int NA = F::NA;
+    const int64_t Vh = g.V >> 1;
+    const PairNbhd nb(g, p);
+    // P_{mu nu}(x) = [U_mu(x) U_nu(x+mu)] [U_nu(x) U_mu(x+nu)]^dag, (mu, nu) = (0,1), (1,2), (2,0)
+#pragma unroll 1
+    for (int mu = 0; mu < 3; ++mu) {
+        const int nu = mu == 2 ? 0 : mu + 1;
+        const M2 t1 = G2::template mulu<false, false>(F::load2(Uin, Vh, mu, p, false),
+                                                      F::load2(Uin, Vh, nu, nb.at(mu, 1), SEAM && nb.swapped(mu, 1)));
+        const M2 t2 = G2::template mulu<false, false>(F::load2(Uin, Vh, nu, p, false),
+                                                      F::load2(Uin, Vh, mu, nb.at(nu, 1), SEAM && nb.swapped(nu, 1)));
+        f2 pr[NA];
+        G2::proj_mul_dag(t1, t2, pr);
+#pragma unroll
+        for (int a = 0; a < NA; ++a) sm[(mu * NA + a) * stride] = pr[a];
+    }
+#pragma unroll 1
+    for (int mu = 0; mu < 3; ++mu) {
+        // lower staples S- = U_nu^dag(x+mu-nu) U_mu^dag(x-nu) U_nu(x-nu)
+        M2 A = G2::zero();
+#pragma unroll
+        for (int k = 1; k <= 2; ++k) {
+            const int nu = mu + k >= 3 ? mu + k - 3 : mu + k;
+            const M2 b1 = F::load2(Uin, Vh, nu, nb.at(mu, 1, nu, -1), SEAM && nb.swapped(mu, 1, nu, -1));
+            const int64_t sb = nb.at(nu, -1);
+            const bool wb = SEAM && nb.swapped(nu, -1);
+            const M2 b2 = F::load2(Uin, Vh, mu, sb, wb);
+            const M2 b3 = F::load2(Uin, Vh, nu, sb, wb);
+            const M2 lo = G2::template mulu<false, false>(G2::template mulu<true, true>(b1, b2), b3);
+            A = G2::add(A, G2::scale(f2(sel3(c.cnu, nu)), lo));
+        }
+        const M2 u = F::load2(Uin, Vh, mu, p, false);
+        f2 e[NA];
+        F::load_e2(E, Vh, mu, p, e);
+        f2 f[NA];
+        G2::proj_mul(u, A, f);
+        const int n1 = mu == 2 ? 0 : mu + 1, n2 = mu == 0 ? 2 : mu - 1;
+        const f2 cp(sel3(c.cnu, n1)), cm(sel3(c.cnu, n2));
+#pragma unroll
+        for (int a = 0; a < NA; ++a) f[a] = fma(cp, sm[(mu * NA + a) * stride], fma(-cm, sm[(n2 * NA + a) * stride], f[a]));
+        const f2 fc(sel3(c.fc, mu));
+        const int mode = MODE >= 0 ? MODE : c.mode;
+        if (mode == MODE_LANGEVIN) {
+            langevin_kick_pair<NA>(cn, mu, p, Vh, step_add, fc, f, e);
+        } else if (mode == MODE_FLOW) {
+#pragma unroll
+            for (int a = 0; a < NA; ++a) e[a] = fc * f[a];
+        } else {
+#pragma unroll
+            for (int a = 0; a < NA; ++a) e[a] = fma(fc, f[a], e[a]);
+        }
+        F::store_e2(E, Vh, mu, p, e);
+        F::store2(Uout, Vh, mu, p, G2::iexp_mul(f2(sel3(c.uc, mu)), e, u));
+    }
 }
 
 // Does the block of pairs [p0, p0 + n) touch the seam planes z = 0 or z = nz/2 - 1?
