@@ -56,6 +56,8 @@ def parse():
     # ensemble = 256 mixed trajectories in batched launches; serve = Poisson request stream
     p.add_argument("--workload", default="leapfrog", choices=["leapfrog", "ensemble", "serve"])
     p.add_argument("--requests", type=int, default=100)
+    p.add_argument("--serve-window", type=float, default=30.0,
+                   help="seconds over which the sustainable serving rate is measured")
     p.add_argument("--trajectories", type=int, default=256)
     return p.parse_args()
 

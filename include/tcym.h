@@ -335,6 +335,14 @@ int tcym_ensemble_destroy(tcym_ensemble ens);
 int tcym_ensemble_add(tcym_ensemble ens, tcym_lattice lat, int dynamics, double dt, double gamma, double T,
                       uint64_t seed, uint64_t step0);
 int tcym_ensemble_remove(tcym_ensemble ens, tcym_lattice lat);
+/* How the ensemble's FP32 site-pair members step (no reference counterpart; the reference runs
+ * each trajectory as its own process).  group_blocks < 0 (the default): one batched launch per
+ * step (graph-captured chunks).  group_blocks >= 0: one persistent launch per chunk of K steps and
+ * coefficient class, whose blocks take (member block, step) work items in order and wait, with a
+ * time limit, only for the member's own previous step; members are cut into groups of at least
+ * group_blocks blocks (0: one group) and a group runs all K steps before the next.
+ * Results are the same bits either way.  Applies from the next tcym_ensemble_step. */
+int tcym_ensemble_set_persistent(tcym_ensemble ens, int group_blocks);
 int tcym_ensemble_size(tcym_ensemble ens, int *n);
 /* Advances every member nsteps steps. */
 int tcym_ensemble_step(tcym_ensemble ens, int nsteps);
@@ -373,6 +381,9 @@ typedef struct {
     uint64_t completed, failed;
     size_t bytes_in_use;
     double link_updates; /* link-updates performed since creation */
+    int preparing;       /* requests whose initial state is being built (or waits for the next tick) */
+    uint64_t ticks;      /* ticks (stride steps of the running ensemble) so far */
+    double prep_seconds; /* host seconds spent preparing initial states, summed over the preparer threads */
 } tcym_server_info;
 int tcym_server_create(tcym_ctx ctx, size_t hbm_budget_bytes, int max_active, int stride, tcym_server *out);
 /* Stops the loop (running requests are abandoned) and frees everything. */
@@ -389,6 +400,10 @@ int tcym_server_wait(tcym_server srv, uint64_t id, double timeout_s);
 int tcym_server_result(tcym_server srv, uint64_t id, double *series, int capacity, int *n_samples,
                        double *latency_s);
 int tcym_server_stats(tcym_server srv, tcym_server_info *out);
+/* The last (up to `capacity`) ticks, oldest first: each tick's wall time in ms (the
+ * ensemble's stride steps and the N_CS sample) and how many requests were being
+ * prepared when it started (either array may be NULL); *n = ticks returned. */
+int tcym_server_ticks(tcym_server srv, double *ms, double *preparing, int capacity, int *n);
 
 #ifdef __cplusplus
 }

@@ -30,8 +30,18 @@ CUDA library draws); every output below is produced by the reference itself:
                            sqrt(0.02): the cumulative DeltaNCsCoolRealTime after
                            each update and the cooled links (SU(3) measurements
                            need LAPACK zgeev, absent here)
+  ref_cooling_su2_96.npz   the SU(2) 96^3 gradient-flow cooling run: U = 1, E ~
+                           N(0, 1/2) (seed 4) restored by the reference, 2000
+                           leapfrog steps of dt 0.05 by the reference, then 500
+                           sweeps of dtau 0.02 with the cooled N_CS along the flow
+                           (improved E.B, trapezoid): simultaneous sweeps by the
+                           reference itself (GradientFlow::CalibrationUpdate) and
+                           checkerboarded sweeps by the oracle's restatement (the
+                           reference has none); (T00, ELECTRIC, MAGNETIC, Delta
+                           N_CS so far) every 10 sweeps, the start's observables and
+                           a few links and fields of the start as its fingerprint
 
-  python tests/golden/make_golden.py
+  python tests/golden/make_golden.py [generator ...]
 """
 import os
 import sys
@@ -219,21 +229,50 @@ def cooling_blocked():
     np.savez_compressed(os.path.join(HERE, "ref_cooling_blocked_su2.npz"), **out)
 
 
+def cooling_su2_96():
+    shape = (96, 96, 96)
+    R = oracle.Ref(2)
+    R.init(shape)
+    R.set_zero()
+    R.thermal_efield(2.0, 4)  # E = N(0,1)/sqrt(2) (seed 4), then Restore
+    R.leapfrog(0.05, 2000)
+    U, E = R.get()
+    rng = np.random.default_rng(96)
+    idx = rng.choice(U.shape[0], size=64, replace=False)
+    out = {"start_obs": R.observables(), "fp_sites": idx, "fp_U": U[idx].copy(), "fp_E": E[idx].copy(),
+           "dtau": 0.02, "every": 10, "sweeps": 500}
+    sim, tot = [], 0.0
+    for _ in range(50):
+        tot += R.flow(np.sqrt(0.02), 10, 1)
+        o = R.observables()
+        sim.append([o[0], o[1], o[2], tot])
+    out["simultaneous"] = np.array(sim)
+    P = oracle.Port(2)
+    cb, tot = [], 0.0
+    for _ in range(50):
+        tot += P.flow_checkerboard_cal(shape, U, E, 0.02, 10, 1)
+        o = P.observables(shape, U, E)
+        cb.append([o[0], o[1], o[2], tot])
+    out["checkerboard"] = np.array(cb)
+    np.savez_compressed(os.path.join(HERE, "ref_cooling_su2_96.npz"), **out)
+
+
+GENERATORS = ("states", "group", "leapfrog_series_su2_16", "thermalize", "cooling", "cooling_blocked", "cooling_su3",
+              "configuration", "cooling_su2_96")
+
+
 if __name__ == "__main__":
     oracle.build()
     if not (oracle.ref_available(2) and oracle.ref_available(3)):
         sys.exit("the reference's sources must be compiled first: make -C oracle ref")
-    for nc in (2, 3):
-        states(nc)
-        group(nc)
-    leapfrog_series_su2_16()
-    for nc in (2, 3):
-        thermalize(nc)
-    cooling()
-    cooling_blocked()
-    cooling_su3()
-    for nc in (2, 3):
-        configuration(nc)
+    which = sys.argv[1:] or GENERATORS  # e.g. `make_golden.py cooling_su2_96` regenerates one fixture
+    for name in which:
+        fn = globals()[name]
+        if name in ("states", "group", "thermalize", "configuration"):
+            for nc in (2, 3):
+                fn(nc)
+        else:
+            fn()
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))

@@ -31,23 +31,25 @@ def random_state(P, nc, shape, seed=3, sigma_u=0.6, sigma_e=0.7):
 @pytest.mark.parametrize("prec", PREC)
 @pytest.mark.parametrize("nc", GROUPS)
 @pytest.mark.parametrize("shape", [(6, 6, 6), (5, 6, 7)])
-def test_leapfrog_parity(ctx, oracle_port, nc, prec, shape):
+@pytest.mark.parametrize("sigma_u", [0.6, 0.3], ids=["rough", "thermal"])
+def test_leapfrog_parity(ctx, oracle_port, nc, prec, shape, sigma_u):
+    """FP64 <= 1e-10, FP32 <= 1e-5 relative.  The rough start (link angles of width
+    0.6) is chaotic enough to amplify FP32 storage rounding ~6x per 50 steps (measured
+    5e-7 at step 10, 9e-6 at step 100), so it is compared through step 10; the start
+    with the configurations' width 0.3 through step 100."""
     P = oracle_port[nc]
-    U, E = random_state(P, nc, shape)
+    U, E = random_state(P, nc, shape, sigma_u=sigma_u)
     lat = tcym.Lattice(ctx, nc, shape, prec)
     lat.set_reunitarize_period(0)
     lat.upload(U, E)
-    for total, nsteps in ((1, 1), (10, 9), (100, 90)):  # cumulative steps at dt = 0.05
+    checks = ((1, 1), (10, 9)) if sigma_u > 0.5 else ((1, 1), (10, 9), (100, 90))  # cumulative steps, dt 0.05
+    for total, nsteps in checks:
         lat.leapfrog(0.05, nsteps)
         P.leapfrog(shape, U, E, 0.05, nsteps)
         Ug, Eg = lat.download()
         tol = TOL[prec]
-        if prec == tcym.FP32 and total == 100:
-            # this rough random start (sigma_U = 0.6) is chaotic enough to amplify the
-            # FP32 storage rounding ~6x per 50 steps (1.3e-6 at step 50, 8e-6..1e-5 at
-            # 100, the same for the host build of the paired and the per-site step);
-            # the configurations' own starts keep 1e-5 over 100 steps (test_gpu_reference_runs)
-            tol = 3e-5
+        print(f"measured leapfrog SU({nc}) {shape} prec={prec} sigma_u={sigma_u} step {total}: "
+              f"U {rel(Ug, U):.2e} E {rel(Eg, E):.2e}")
         assert rel(Ug, U) < tol, (total, rel(Ug, U))
         assert rel(Eg, E) < tol, (total, rel(Eg, E))
 
@@ -276,9 +278,11 @@ def test_thermalize_parity(ctx, oracle_port, nc, prec):
     lat.set_zero()
     series = lat.thermalize(2.0, 7, 2, 0.75, 0.0375, every=5)
     assert series.shape == ref.shape == (8, 7)
-    tol = TOL[prec] if prec == tcym.FP64 else 2e-5  # FP32 restores to 1e-6 before the steps
-    assert np.abs(series - ref).max() <= tol * np.abs(ref).max()
+    tol = TOL[prec]  # measured FP32: series 2e-7, fields 9e-7
     Ug, Eg = lat.download()
+    print(f"\nmeasured thermalize SU({nc}) prec={prec}: series {np.abs(series - ref).max() / np.abs(ref).max():.2e} "
+          f"U {rel(Ug, U):.2e} E {rel(Eg, E):.2e}")
+    assert np.abs(series - ref).max() <= tol * np.abs(ref).max()
     assert rel(Ug, U) < tol and rel(Eg, E) < tol
 
 
@@ -312,12 +316,15 @@ def test_cooled_delta_ncs_parity(ctx, oracle_port, nc, prec):
         total += d
         scale = max(scale, abs(d))
         got = cool.update(True)
-        tol = 1e-9 if prec == tcym.FP64 else 1e-3
+        # a sum that cancels: relative to the largest increment (measured FP32: 1.0e-6 of it)
+        tol = 1e-9 if prec == tcym.FP64 else 1e-5
+        print(f"measured cooled Delta N_CS SU({nc}) prec={prec}: |got-d| {abs(got - d):.2e} "
+              f"scale {max(scale, 1e-3):.2e} total {abs(cool.total() - total):.2e}")
         assert abs(got - d) <= tol * max(scale, 1e-3), (got, d)
         assert abs(cool.total() - total) <= 3 * tol * max(scale, 1e-3)
         old = new
     ref2 = P.cooled_delta_ncs(shape, old, new, 2)
-    assert abs(cool.delta_ncs(2) - ref2) <= (1e-9 if prec == tcym.FP64 else 1e-3) * max(abs(ref2), 1e-3)
+    assert abs(cool.delta_ncs(2) - ref2) <= (1e-9 if prec == tcym.FP64 else 1e-5) * max(abs(ref2), 1e-3)
     cool.close()
 
 

@@ -33,8 +33,9 @@ def rel(a, b):
     return float(np.abs(a - b).max() / np.abs(b).max())
 
 
-# tolerances: (energies, E.B) relative to max(1, |value|)
-@pytest.mark.parametrize("prec,tol_e,tol_edb", [(tcym.FP64, 1e-10, 1e-8), (tcym.FP32, 2e-5, 2e-3)])
+# tolerances: energies relative; E.B (a sum that cancels) relative to its mean magnitude over
+# the compared records, FP32 10x the measured 2.0e-6
+@pytest.mark.parametrize("prec,tol_e,tol_edb", [(tcym.FP64, 1e-10, 1e-10), (tcym.FP32, 1e-5, 2e-5)])
 def test_su2_16_leapfrog_against_reference_series(ctx, prec, tol_e, tol_edb):
     d = dict(np.load(os.path.join(G, "ref_leapfrog_su2_16.npz")))
     s = d["series"]
@@ -49,6 +50,8 @@ def test_su2_16_leapfrog_against_reference_series(ctx, prec, tol_e, tol_edb):
         lat = tcym.Lattice(ctx, 2, shape, prec)
         lat.copy_from(ic)
     T00 = []
+    edb_scale = np.abs(s[:11, 13]).mean()
+    err_e = err_edb = 0.0
     for rec in range(len(s)):
         if rec:
             lat.leapfrog(float(d["dt"]), int(d["every"]))
@@ -57,10 +60,14 @@ def test_su2_16_leapfrog_against_reference_series(ctx, prec, tol_e, tol_edb):
         T00.append(v[0])
         if rec <= 10:  # the first 100 steps: pointwise
             for k in (0, 1, 2):
-                assert abs(v[k] - s[rec][k]) <= tol_e * max(1.0, abs(s[rec][k])), (rec, k, v[k], s[rec][k])
-            assert abs(v[13] - s[rec][13]) <= tol_edb * max(1.0, abs(s[rec][13])), (rec, v[13], s[rec][13])
+                if s[rec][k] != 0.0:  # the magnetic energy of the unit-link start is exactly 0
+                    err_e = max(err_e, abs(v[k] - s[rec][k]) / abs(s[rec][k]))
+                assert abs(v[k] - s[rec][k]) <= tol_e * abs(s[rec][k]) + 1e-15, (rec, k, v[k], s[rec][k])
+            err_edb = max(err_edb, abs(v[13] - s[rec][13]) / edb_scale)
+            assert abs(v[13] - s[rec][13]) <= tol_edb * edb_scale, (rec, v[13], s[rec][13])
         assert o.gauss_absmax < (1e-11 if prec == tcym.FP64 else 1e-4)
         assert o.unit_max < (1e-12 if prec == tcym.FP64 else 1e-5)
+    print(f"\nmeasured SU(2) 16^3 series prec={prec}: energies {err_e:.2e}, E.B / mean |E.B| {err_edb:.2e}")
     T00, Tref = np.array(T00), s[:, 0]
     # beyond the chaotic horizon both conserve the energy: they agree to the leapfrog fluctuation
     assert np.abs(T00[20:] - Tref[20:]).max() < 5e-3 * Tref.mean()
@@ -106,8 +113,10 @@ def _cooling_input(ctx, shape, nlf, tol=1e-14):
     return lat
 
 
-@pytest.mark.parametrize("prec,tol", [(tcym.FP64, 1e-10), (tcym.FP32, 2e-5)])
-def test_su2_cooling_sweeps_against_oracle(ctx, oracle_port, prec, tol):
+# links relative; the magnetic energy, which cooling drives down (so its relative error
+# grows), FP32 to 5e-5 (6x the measured 8.3e-6)
+@pytest.mark.parametrize("prec,tol,tol_mag", [(tcym.FP64, 1e-10, 1e-9), (tcym.FP32, 1e-5, 5e-5)])
+def test_su2_cooling_sweeps_against_oracle(ctx, oracle_port, prec, tol, tol_mag):
     P = oracle_port[2]
     shape = (32, 32, 32)
     src = _cooling_input(ctx, shape, 200)
@@ -124,7 +133,7 @@ def test_su2_cooling_sweeps_against_oracle(ctx, oracle_port, prec, tol):
         assert rel(Ug, U) < tol, (sweep, rel(Ug, U))
         o = lat.observables().as_oracle_vector()
         r = P.observables(shape, U, E)
-        assert abs(o[2] - r[2]) <= 10 * tol * r[2]
+        assert abs(o[2] - r[2]) <= tol_mag * r[2]
         mags.append(o[2])
     assert all(b < a for a, b in zip(mags, mags[1:]))  # cooling lowers the magnetic energy
 
@@ -172,7 +181,8 @@ def test_energy_drift_fp32_vs_fp64(ctx):
     assert l32.observables().unit_max < 1e-5  # periodic FP64 reunitarisation keeps FP32 links on the group
 
 
-@pytest.mark.parametrize("prec,tol", [(tcym.FP64, 1e-9), (tcym.FP32, 1e-4)])
+# relative to the largest increment of the series (it cancels): FP32 10x the measured 4.0e-7
+@pytest.mark.parametrize("prec,tol", [(tcym.FP64, 1e-9), (tcym.FP32, 4e-6)])
 def test_su2_cooled_ncs_series(ctx, oracle_port, prec, tol):
     """The cooling run's cooled N_CS: Delta N_CS accumulated along the gradient flow as
     GradientFlow::CalibrationUpdate does (GradientFlow.cpp:168-188, improved E.B),

@@ -84,7 +84,8 @@ class _Request(ctypes.Structure):
 
 class _ServerInfo(ctypes.Structure):
     _fields_ = [("queued", ctypes.c_int), ("active", ctypes.c_int), ("completed", ctypes.c_uint64),
-                ("failed", ctypes.c_uint64), ("bytes_in_use", ctypes.c_size_t), ("link_updates", ctypes.c_double)]
+                ("failed", ctypes.c_uint64), ("bytes_in_use", ctypes.c_size_t), ("link_updates", ctypes.c_double),
+                ("preparing", ctypes.c_int), ("ticks", ctypes.c_uint64), ("prep_seconds", ctypes.c_double)]
 
 
 _LIB = None
@@ -175,6 +176,7 @@ def library() -> ctypes.CDLL:
         "tcym_ensemble_add": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                ctypes.c_double, ctypes.c_uint64, ctypes.c_uint64], ctypes.c_int),
         "tcym_ensemble_remove": ([ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+        "tcym_ensemble_set_persistent": ([ctypes.c_void_p, ctypes.c_int], ctypes.c_int),
         "tcym_ensemble_size": ([ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
         "tcym_ensemble_step": ([ctypes.c_void_p, ctypes.c_int], ctypes.c_int),
         "tcym_ensemble_measure": ([ctypes.c_void_p, ctypes.c_int, _dp, _dp], ctypes.c_int),
@@ -189,6 +191,7 @@ def library() -> ctypes.CDLL:
         "tcym_server_result": ([ctypes.c_void_p, ctypes.c_uint64, _dp, ctypes.c_int, ctypes.POINTER(ctypes.c_int),
                                 _dp], ctypes.c_int),
         "tcym_server_stats": ([ctypes.c_void_p, ctypes.POINTER(_ServerInfo)], ctypes.c_int),
+        "tcym_server_ticks": ([ctypes.c_void_p, _dp, _dp, ctypes.c_int, ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -563,6 +566,11 @@ class Ensemble:
         self.ctx.check(self.lib.tcym_ensemble_add(self.h, lat.h, dynamics, dt, gamma, T, seed, step0))
         self.members.append(lat)
 
+    def set_persistent(self, group_blocks: int = 0):
+        """K-step persistent launches (group_blocks >= 0, members in groups of at least that
+        many blocks; 0: one group) or one launch per step (group_blocks < 0)."""
+        self.ctx.check(self.lib.tcym_ensemble_set_persistent(self.h, group_blocks))
+
     def remove(self, lat: Lattice):
         self.ctx.check(self.lib.tcym_ensemble_remove(self.h, lat.h))
         self.members.remove(lat)
@@ -637,6 +645,13 @@ class Server:
         s = _ServerInfo()
         self.ctx.check(self.lib.tcym_server_stats(self.h, ctypes.byref(s)))
         return {k: getattr(s, k) for k, _ in _ServerInfo._fields_}
+
+    def ticks(self, capacity: int = 8192):
+        """(ms, preparing) arrays of the last ticks, oldest first."""
+        ms, prep, n = np.zeros(capacity), np.zeros(capacity), ctypes.c_int()
+        self.ctx.check(self.lib.tcym_server_ticks(self.h, ms.ctypes.data_as(_dp), prep.ctypes.data_as(_dp), capacity,
+                                                  ctypes.byref(n)))
+        return ms[: n.value], prep[: n.value]
 
     def close(self):
         if self.h:

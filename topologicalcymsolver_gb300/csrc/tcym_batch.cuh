@@ -39,8 +39,13 @@ template <class T> struct Member {
 #ifndef TCYM_SU2_BATCH_MINBLOCKS
 #define TCYM_SU2_BATCH_MINBLOCKS 6
 #endif
+// SU(3) likewise: at 4 blocks (128 registers) the table-reading step spills
+#ifndef TCYM_SU3_BATCH_MINBLOCKS
+#define TCYM_SU3_BATCH_MINBLOCKS 3
+#endif
 template <int FMT> constexpr int batch_min_blocks_for() {
     if constexpr (Fmt<FMT>::PAIRED && Fmt<FMT>::NA == 3) return TCYM_SU2_BATCH_MINBLOCKS;
+    if constexpr (Fmt<FMT>::PAIRED && Fmt<FMT>::NA == 8) return TCYM_SU3_BATCH_MINBLOCKS;
     return Fmt<FMT>::PAIRED ? pair_min_blocks_for<FMT>() : min_blocks_for<FMT>();
 }
 
@@ -63,6 +68,12 @@ template <int FMT, bool GENERAL>
 __global__ void __launch_bounds__(threads_for<FMT>(), batch_min_blocks_for<FMT>())
     k_step_batch(const Member<typename Fmt<FMT>::T> *__restrict__ members, int nmembers, int total_blocks, int k) {
     static_assert(!Fmt<FMT>::PAIRED || threads_for<FMT>() == kThreadsPair, "one block shape for both paths");
+    using T = typename Fmt<FMT>::T;
+    // each thread's plaquette slots (its own only: no thread reads another's); the
+    // per-site path of an FP32 member uses the same array as floats
+    using S = typename std::conditional<Fmt<FMT>::PAIRED, f2, T>::type;
+    __shared__ S sm_pair[plaq_slots<FMT>() * threads_for<FMT>()];
+    T *const sm_site = reinterpret_cast<T *>(sm_pair);
     for (int item = blockIdx.x; item < total_blocks; item += gridDim.x) {
         const int mi = find_member(members, nmembers, item, false);
         // the table is read-only and never aliases the fields (__restrict__), so
@@ -75,9 +86,11 @@ __global__ void __launch_bounds__(threads_for<FMT>(), batch_min_blocks_for<FMT>(
             if (p < (g.V >> 1)) {
                 const int in = m.cur ^ (k & 1);
                 if (pairs_touch_seam(g, p0, kThreadsPair))
-                    site_step_pair<Fmt<FMT>, true>(g, m.U[in], m.U[in ^ 1], m.E, m.c, p, (uint64_t)k);
+                    site_step_pair<Fmt<FMT>, true>(g, m.U[in], m.U[in ^ 1], m.E, m.c, p, (uint64_t)k,
+                                                   sm_pair + threadIdx.x, kThreadsPair);
                 else
-                    site_step_pair<Fmt<FMT>, false>(g, m.U[in], m.U[in ^ 1], m.E, m.c, p, (uint64_t)k);
+                    site_step_pair<Fmt<FMT>, false>(g, m.U[in], m.U[in ^ 1], m.E, m.c, p, (uint64_t)k,
+                                                    sm_pair + threadIdx.x, kThreadsPair);
             }
             continue;
         }
@@ -87,8 +100,12 @@ __global__ void __launch_bounds__(threads_for<FMT>(), batch_min_blocks_for<FMT>(
                 bool seam;
                 if (tile_pair(g, m.tile, item - m.block_begin, threadIdx.x, p, seam)) {
                     const int in = m.cur ^ (k & 1);
-                    if (seam) site_step_pair<Fmt<FMT>, true>(g, m.U[in], m.U[in ^ 1], m.E, m.c, p, (uint64_t)k);
-                    else site_step_pair<Fmt<FMT>, false>(g, m.U[in], m.U[in ^ 1], m.E, m.c, p, (uint64_t)k);
+                    if (seam)
+                        site_step_pair<Fmt<FMT>, true>(g, m.U[in], m.U[in ^ 1], m.E, m.c, p, (uint64_t)k,
+                                                       sm_pair + threadIdx.x, kThreadsPair);
+                    else
+                        site_step_pair<Fmt<FMT>, false>(g, m.U[in], m.U[in ^ 1], m.E, m.c, p, (uint64_t)k,
+                                                        sm_pair + threadIdx.x, kThreadsPair);
                 }
                 continue;
             }
@@ -96,7 +113,8 @@ __global__ void __launch_bounds__(threads_for<FMT>(), batch_min_blocks_for<FMT>(
         const int64_t s = (int64_t)(item - m.block_begin) * blockDim.x + threadIdx.x;
         if (s < g.V) {
             const int in = m.cur ^ (k & 1);
-            site_step<Fmt<FMT>, true, true>(g, m.U[in], m.U[in ^ 1], m.E, m.c, s, (uint64_t)k);
+            site_step<Fmt<FMT>, true, true>(g, m.U[in], m.U[in ^ 1], m.E, m.c, s, (uint64_t)k,
+                                            sm_site + threadIdx.x, (int)blockDim.x);
         }
     }
 }
@@ -114,6 +132,7 @@ __global__ void __launch_bounds__(kThreadsPair, pair_min_blocks_for<FMT>())
     k_step_batch_uniform(const Member<float> *__restrict__ members, int nmembers, int item0, int total_blocks, int k,
                          StepCoef<float> c) {
     static_assert(Fmt<FMT>::PAIRED, "paired formats only");
+    __shared__ f2 sm[plaq_slots<FMT>() * kThreadsPair];
 #if TCYM_BATCH_PERSISTENT
     for (int item = item0 + blockIdx.x; item < total_blocks; item += gridDim.x) {
 #else
@@ -128,9 +147,109 @@ __global__ void __launch_bounds__(kThreadsPair, pair_min_blocks_for<FMT>())
         if (p < (g.V >> 1)) {
             const int in = m.cur ^ (k & 1);
             if (pairs_touch_seam(g, p0, kThreadsPair))
-                site_step_pair<Fmt<FMT>, true>(g, m.U[in], m.U[in ^ 1], m.E, c, m.c, p, (uint64_t)k);
+                site_step_pair<Fmt<FMT>, true>(g, m.U[in], m.U[in ^ 1], m.E, c, m.c, p, (uint64_t)k,
+                                               sm + threadIdx.x, kThreadsPair);
             else
-                site_step_pair<Fmt<FMT>, false>(g, m.U[in], m.U[in ^ 1], m.E, c, m.c, p, (uint64_t)k);
+                site_step_pair<Fmt<FMT>, false>(g, m.U[in], m.U[in ^ 1], m.E, c, m.c, p, (uint64_t)k,
+                                                sm + threadIdx.x, kThreadsPair);
+        }
+    }
+}
+
+// ---------------------------------------------------------------- persistent
+// K steps of one coefficient class in a single launch.  The class's work items
+// (one block of 128 site pairs of one member at one step) are handed out by an
+// atomic counter in a fixed order: the members are cut into groups, and a group
+// runs all K steps before the next group starts, step by step within the group.
+// A group small enough keeps its links and fields in the 129 MB L2 across its
+// steps, where one launch per step streams every member through DRAM each step.
+//
+// The item of step k of member m waits until all of m's step k-1 items are done
+// (a per-member counter, raised by each finished item with release semantics;
+// the waiter reads it, fences and releases its block with a barrier, the
+// pattern of a grid-wide barrier).  The wait cannot deadlock and needs no
+// co-resident grid: items are taken in increasing order and only ever wait for
+// items taken earlier, so the oldest unfinished item can always run.  Each wait
+// gives up after `spin_limit` clock cycles: it raises the error flag, every
+// block then stops taking items, and the host reports a timeout.
+//
+// ctl: [0] next item, [1] error flag, [2 + i] items done of member i.  A member's
+// arithmetic is that of the other step kernels.
+struct PersistentPlan {
+    const int *sched;  // [0, ngroups]: first item of group g; [ngroups + 1, 2 ngroups + 1]: its first block
+    int ngroups;
+    int K;
+    int item0, item1;  // the class's blocks in the format's block numbering
+    long long spin_limit;
+};
+
+__device__ __forceinline__ int find_group(const int *first_item, int ngroups, int item) {
+    int lo = 0, hi = ngroups - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (first_item[mid] <= item) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+template <int FMT>
+__global__ void __launch_bounds__(kThreadsPair, batch_min_blocks_for<FMT>())
+    k_step_persistent(const Member<float> *__restrict__ members, int nmembers, PersistentPlan plan,
+                      StepCoef<float> c, int *ctl) {
+    static_assert(Fmt<FMT>::PAIRED, "paired formats only");
+    __shared__ f2 sm[plaq_slots<FMT>() * kThreadsPair];
+    __shared__ int s_item, s_stop;
+    const int *first_item = plan.sched, *first_block = plan.sched + plan.ngroups + 1;
+    const int total = first_item[plan.ngroups];
+    for (;;) {
+        if (threadIdx.x == 0) {
+            const int it = atomicAdd(&ctl[0], 1);
+            s_item = *(volatile int *)&ctl[1] ? total : it;
+        }
+        __syncthreads();
+        const int item = s_item;
+        if (item >= total) return;
+        const int g = find_group(first_item, plan.ngroups, item);
+        const int nbg = first_block[g + 1] - first_block[g];
+        const int rel = item - first_item[g];
+        const int k = rel / nbg;
+        const int blk = plan.item0 + first_block[g] + (rel - k * nbg);
+        const int mi = find_member(members, nmembers, blk, false);
+        const Member<float> &m = members[mi];
+        if (k > 0) {
+            if (threadIdx.x == 0) {
+                const int nblk = (mi + 1 < nmembers ? members[mi + 1].block_begin : plan.item1) - m.block_begin;
+                const int need = k * nblk;
+                const long long t0 = clock64();
+                int stop = 0;
+                while (*(volatile int *)&ctl[2 + mi] < need) {
+                    if (*(volatile int *)&ctl[1] || clock64() - t0 > plan.spin_limit) {
+                        atomicExch(&ctl[1], 1);
+                        stop = 1;
+                        break;
+                    }
+                }
+                __threadfence();
+                s_stop = stop;
+            }
+            __syncthreads();
+            if (s_stop) return;
+        }
+        const Geom g0 = m.g;
+        const int64_t p0 = (int64_t)(blk - m.block_begin) * kThreadsPair, p = p0 + threadIdx.x;
+        if (p < (g0.V >> 1)) {
+            const int in = m.cur ^ (k & 1);
+            if (pairs_touch_seam(g0, p0, kThreadsPair))
+                site_step_pair<Fmt<FMT>, true>(g0, m.U[in], m.U[in ^ 1], m.E, c, m.c, p, (uint64_t)k,
+                                               sm + threadIdx.x, kThreadsPair);
+            else
+                site_step_pair<Fmt<FMT>, false>(g0, m.U[in], m.U[in ^ 1], m.E, c, m.c, p, (uint64_t)k,
+                                                sm + threadIdx.x, kThreadsPair);
+        }
+        __syncthreads();  // every thread's stores are issued (and s_item may be reused)
+        if (threadIdx.x == 0) {
+            __threadfence();
+            atomicAdd(&ctl[2 + mi], 1);
         }
     }
 }
@@ -204,6 +323,21 @@ template <int FMT> struct LaunchBatch {
         if constexpr (Fmt<FMT>::PAIRED) {
             k_step_batch_uniform<FMT><<<item1 - item0, TPB, 0, st>>>(members + m0, n, item0, item1, k,
                                                                     coef_cast<float>(cu));
+            return cudaGetLastError();
+        }
+        return cudaErrorInvalidValue;
+    }
+    // the persistent K-step launch of one coefficient class (k_step_persistent)
+    static int persistent_resident_blocks() {
+        int b = 0;
+        if constexpr (Fmt<FMT>::PAIRED)
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_step_persistent<FMT>, kThreadsPair, 0);
+        return b > 0 ? b : 1;
+    }
+    static cudaError_t step_persistent(const Member<T> *members, int m0, int n, const PersistentPlan &plan,
+                                       const StepCoef<double> &cu, int *ctl, int grid, cudaStream_t st) {
+        if constexpr (Fmt<FMT>::PAIRED) {
+            k_step_persistent<FMT><<<grid, kThreadsPair, 0, st>>>(members + m0, n, plan, coef_cast<float>(cu), ctl);
             return cudaGetLastError();
         }
         return cudaErrorInvalidValue;

@@ -3,6 +3,7 @@
 // lattice's stream; all arithmetic is in the kernels.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -148,18 +149,31 @@ static void drop_host_graphs(tcym_lattice lat) {
     }
 }
 
+cudaError_t tcym_lattice_alloc(tcym_lattice lat, void **p, size_t bytes) {
+    if (lat->pool) return cudaMallocFromPoolAsync(p, bytes, lat->pool, lat->stream);
+    return cudaMalloc(p, bytes);
+}
+void tcym_lattice_free_mem(tcym_lattice lat, void *p) {
+    if (!p) return;
+    if (lat->pool) cudaFreeAsync(p, lat->stream);
+    else cudaFree(p);
+}
+
 static void lattice_free(tcym_lattice lat) {
     cudaSetDevice(lat->ctx->device);
     if (lat->stream) cudaStreamSynchronize(lat->stream);
     drop_host_graphs(lat);
-    cudaFree(lat->U[0]);
-    cudaFree(lat->U[1]);
-    cudaFree(lat->E);
-    cudaFree(lat->partial);
-    cudaFree(lat->result);
-    cudaFree(lat->gauss);
-    cudaFree(lat->staging);
-    if (lat->host_result) cudaFreeHost(lat->host_result);
+    tcym_lattice_free_mem(lat, lat->U[0]);
+    tcym_lattice_free_mem(lat, lat->U[1]);
+    tcym_lattice_free_mem(lat, lat->E);
+    tcym_lattice_free_mem(lat, lat->partial);
+    tcym_lattice_free_mem(lat, lat->result);
+    tcym_lattice_free_mem(lat, lat->gauss);
+    tcym_lattice_free_mem(lat, lat->staging);
+    if (lat->host_result) {
+        if (lat->pool) std::free(lat->host_result);
+        else cudaFreeHost(lat->host_result);
+    }
     for (int i = 0; i < 2; ++i)
         if (lat->side[i]) cudaStreamDestroy(lat->side[i]);
     for (int i = 0; i < 3; ++i)
@@ -171,8 +185,8 @@ static void lattice_free(tcym_lattice lat) {
     if (lat->stream) cudaStreamDestroy(lat->stream);
 }
 
-extern "C" int tcym_lattice_create_ex(tcym_ctx ctx, int nc, int nx, int ny, int nz, const double a[3], int precision,
-                                      tcym_lattice *out) {
+static int lattice_create(tcym_ctx ctx, int nc, int nx, int ny, int nz, const double a[3], int precision,
+                          cudaMemPool_t pool, tcym_lattice *out) {
     if (!ctx || !out) return TCYM_ERR_ARG;
     *out = nullptr;
     if ((nc != 2 && nc != 3) || (precision != TCYM_FP32 && precision != TCYM_FP64) || nx < 2 || ny < 2 || nz < 2) {
@@ -202,22 +216,39 @@ extern "C" int tcym_lattice_create_ex(tcym_ctx ctx, int nc, int nx, int ny, int 
     };
     cudaError_t e;
     if ((e = cudaStreamCreateWithFlags(&lat->stream, cudaStreamNonBlocking)) != cudaSuccess) return fail(e, "stream");
+    lat->pool = pool;
     const size_t nst = tcym_stored_sites(lat->fmt, V);
     const size_t ub = 3 * tcym_link_bytes(lat->fmt) * nst, eb = 3 * tcym_field_bytes(lat->fmt) * nst;
-    if ((e = cudaMalloc(&lat->U[0], ub)) != cudaSuccess) return fail(e, "cudaMalloc(U)");
-    if ((e = cudaMalloc(&lat->U[1], ub)) != cudaSuccess) return fail(e, "cudaMalloc(U')");
-    if ((e = cudaMalloc(&lat->E, eb)) != cudaSuccess) return fail(e, "cudaMalloc(E)");
+    auto alloc = [&](void **p, size_t n) { return tcym_lattice_alloc(lat, p, n); };
+    if ((e = alloc(&lat->U[0], ub)) != cudaSuccess) return fail(e, "allocation of U");
+    if ((e = alloc(&lat->U[1], ub)) != cudaSuccess) return fail(e, "allocation of U'");
+    if ((e = alloc(&lat->E, eb)) != cudaSuccess) return fail(e, "allocation of E");
     lat->max_blocks = ctx->sm_count * 8;
-    if ((e = cudaMalloc(&lat->partial, sizeof(double) * P_WIDTH * lat->max_blocks)) != cudaSuccess)
-        return fail(e, "cudaMalloc(partial)");
-    if ((e = cudaMalloc(&lat->result, sizeof(double) * R_WIDTH)) != cudaSuccess) return fail(e, "cudaMalloc(result)");
+    if ((e = alloc((void **)&lat->partial, sizeof(double) * P_WIDTH * lat->max_blocks)) != cudaSuccess)
+        return fail(e, "allocation of the reduction records");
+    if ((e = alloc((void **)&lat->result, sizeof(double) * R_WIDTH)) != cudaSuccess)
+        return fail(e, "allocation of the result block");
     if ((e = cudaMemsetAsync(lat->result, 0, sizeof(double) * R_WIDTH, lat->stream)) != cudaSuccess)
         return fail(e, "memset(result)");
-    if ((e = cudaMallocHost(&lat->host_result, sizeof(double) * R_WIDTH)) != cudaSuccess)
+    if (pool) {
+        lat->host_result = static_cast<double *>(std::calloc(R_WIDTH, sizeof(double)));
+        if (!lat->host_result) return fail(cudaErrorMemoryAllocation, "host result block");
+    } else if ((e = cudaMallocHost(&lat->host_result, sizeof(double) * R_WIDTH)) != cudaSuccess) {
         return fail(e, "cudaMallocHost(result)");
+    }
     lat->bytes = 2 * ub + eb + sizeof(double) * (P_WIDTH * lat->max_blocks + R_WIDTH);
     *out = lat;
     return TCYM_OK;
+}
+
+extern "C" int tcym_lattice_create_ex(tcym_ctx ctx, int nc, int nx, int ny, int nz, const double a[3], int precision,
+                                      tcym_lattice *out) {
+    return lattice_create(ctx, nc, nx, ny, nz, a, precision, nullptr, out);
+}
+
+int tcym_lattice_create_pooled(tcym_ctx ctx, int nc, int nx, int ny, int nz, int precision, cudaMemPool_t pool,
+                               tcym_lattice *out) {
+    return lattice_create(ctx, nc, nx, ny, nz, nullptr, precision, pool, out);
 }
 
 extern "C" int tcym_lattice_create(tcym_ctx ctx, int nc, int nx, int ny, int nz, int precision, tcym_lattice *out) {
@@ -231,9 +262,15 @@ extern "C" int tcym_lattice_destroy(tcym_lattice lat) {
     return TCYM_OK;
 }
 
+// Doubles of a lattice's restore scratch: the violation array G[a*V + s] and the
+// restore's control block (first iteration not to run, non-finite flag, spare).
+static size_t gauss_scratch_doubles(const tcym_lattice_s *lat) {
+    return (size_t)(lat->nc == 2 ? 3 : 8) * (size_t)lat->g.V + 4;
+}
+
 extern "C" int tcym_lattice_bytes(tcym_lattice lat, size_t *bytes) {
     if (!lat || !bytes) return TCYM_ERR_ARG;
-    *bytes = lat->bytes + lat->staging_bytes + (lat->gauss ? sizeof(double) * 8 * (size_t)lat->g.V : 0);
+    *bytes = lat->bytes + lat->staging_bytes + (lat->gauss ? sizeof(double) * gauss_scratch_doubles(lat) : 0);
     return TCYM_OK;
 }
 
@@ -247,10 +284,10 @@ static int ensure_staging(tcym_lattice lat) {
         if (!lat->ev[i]) CK(cudaEventCreateWithFlags(&lat->ev[i], cudaEventDisableTiming));
     if (lat->staging_bytes >= need) return TCYM_OK;
     drop_host_graphs(lat);
-    cudaFree(lat->staging);
+    tcym_lattice_free_mem(lat, lat->staging);
     lat->staging = nullptr;
     lat->staging_bytes = 0;
-    CK(cudaMalloc(&lat->staging, need));
+    CK(tcym_lattice_alloc(lat, (void **)&lat->staging, need));
     lat->staging_bytes = need;
     return TCYM_OK;
 }
@@ -404,8 +441,8 @@ void tcym_lattice_release_scratch(tcym_lattice lat) {
     cudaSetDevice(lat->ctx->device);
     cudaStreamSynchronize(lat->stream);
     drop_host_graphs(lat);
-    cudaFree(lat->gauss);
-    cudaFree(lat->staging);
+    tcym_lattice_free_mem(lat, lat->gauss);
+    tcym_lattice_free_mem(lat, lat->staging);
     lat->gauss = nullptr;
     lat->staging = nullptr;
     lat->staging_bytes = 0;
@@ -481,51 +518,62 @@ static int fetch_result(tcym_lattice lat) {
     return TCYM_OK;
 }
 
+// GaussLawRestoration::Restore (GAUSSLAWFIXING/GaussRestore.cpp:131-167).  Each
+// iteration is three (deviation, update) sub-steps; the reference stops once the
+// signed maximum of the third deviation is <= tol (GaussRestore.cpp:150).  The
+// iterations are queued in growing batches between host checks: the finaliser of
+// the deciding deviation writes the stopping iteration into the device control
+// block, and the kernels of later iterations return at once, so the result, the
+// iteration count and the final maximum are those of the reference's loop, with
+// one host synchronisation per batch instead of one per iteration.  The result
+// block's non-finite flag (sticky) is cleared first: the restore judges only its
+// own reductions, and their sums see a NaN that the signed maximum drops.
 extern "C" int tcym_gauss_restore(tcym_lattice lat, double tol, int maxit, int *iters, double *final_max) {
     TCYM_RANGE("tcym_gauss_restore");
     if (!lat || maxit < 0) return TCYM_ERR_ARG;
     tcym_ctx ctx = lat->ctx;
     cudaSetDevice(ctx->device);
     const int na = lat->nc == 2 ? 3 : 8;
-    if (!lat->gauss) CK(cudaMalloc(&lat->gauss, sizeof(double) * na * (size_t)lat->g.V));
+    if (!lat->gauss) CK(tcym_lattice_alloc(lat, (void **)&lat->gauss, sizeof(double) * gauss_scratch_doubles(lat)));
+    double *ctl = lat->gauss + (size_t)na * (size_t)lat->g.V;
     const double gam[3] = {7.0 / 24.0, 7.0 / 48.0, 7.0 / 72.0};
     int blocks = 0;
     DISPATCH(lat->fmt, blocks = L::reduce_grid(lat->g, lat->max_blocks));
-    auto deviation = [&]() -> int {
-        DISPATCH(lat->fmt, CK(L::gauss_compute(lat->g, lat->U[lat->cur], lat->E, lat->gauss, lat->partial, blocks,
-                                               lat->stream)));
-        CK(finalize_obs(lat->partial, blocks, na, lat->g.V, 0.0, lat->result, lat->stream));
+    CK(cudaMemsetAsync(lat->result + R_NONFINITE, 0, sizeof(double), lat->stream));
+    const double init[4] = {(double)maxit, 0.0, 0.0, 0.0};
+    CK(cudaMemcpyAsync(ctl, init, sizeof(init), cudaMemcpyHostToDevice, lat->stream));
+    auto deviation = [&](int it, bool check) -> int {
+        DISPATCH(lat->fmt, CK(L::gauss_compute_it(lat->g, lat->U[lat->cur], lat->E, lat->gauss, lat->partial, blocks,
+                                                  ctl, it, lat->stream)));
+        CK(finalize_restore(lat->partial, blocks, na, lat->g.V, lat->result, ctl, tol, it, check, lat->stream));
         return TCYM_OK;
     };
-    // The result block's non-finite flag is sticky; the restore judges only its
-    // own reductions, so it starts from a clear flag.  The signed maximum alone
-    // would miss a NaN (fmax drops it); the flag sees it in the sums.
-    CK(cudaMemsetAsync(lat->result + R_NONFINITE, 0, sizeof(double), lat->stream));
-    auto nonfinite = [&](int at) -> bool {
-        if (lat->host_result[R_NONFINITE] == 0.0 && std::isfinite(lat->host_result[R_GMAX])) return false;
-        tcym_set_error(ctx, "tcym_gauss_restore: non-finite violation at iteration %d", at);
-        return true;
-    };
     // initial deviation (GaussRestore.cpp:143)
-    int r = deviation();
+    int r = deviation(-1, true);
     if (r) return r;
-    if ((r = fetch_result(lat))) return r;
-    if (nonfinite(0)) return TCYM_ERR_NONFINITE;
-    double gmax = lat->host_result[R_GMAX];
-    int it = 0;
-    while (it < maxit && gmax > tol) {
-        for (int k = 0; k < 3; ++k) {
-            if ((r = deviation())) return r;
-            DISPATCH(lat->fmt,
-                     CK(L::gauss_update(lat->g, lat->U[lat->cur], lat->E, lat->gauss, gam[k], lat->stream)));
+    double h[4];
+    int queued = 0, batch = 4, stop = maxit;
+    for (;;) {
+        CK(cudaMemcpyAsync(h, ctl, sizeof(h), cudaMemcpyDeviceToHost, lat->stream));
+        if ((r = fetch_result(lat))) return r;  // synchronises the stream
+        stop = (int)h[0];
+        if (h[1] != 0.0) {
+            tcym_set_error(ctx, "tcym_gauss_restore: non-finite violation at iteration %d", stop - 1);
+            return TCYM_ERR_NONFINITE;
         }
-        if ((r = fetch_result(lat))) return r;  // max of the last deviation, as the reference tests it
-        gmax = lat->host_result[R_GMAX];
-        if (nonfinite(it)) return TCYM_ERR_NONFINITE;
-        ++it;
+        if (stop <= queued || queued >= maxit) break;
+        const int n = std::min(batch, maxit - queued);
+        for (int it = queued; it < queued + n; ++it)
+            for (int k = 0; k < 3; ++k) {
+                if ((r = deviation(it, k == 2))) return r;
+                DISPATCH(lat->fmt, CK(L::gauss_update_it(lat->g, lat->U[lat->cur], lat->E, lat->gauss, gam[k], ctl, it,
+                                                         lat->stream)));
+            }
+        queued += n;
+        batch = std::min(2 * batch, 64);
     }
-    if (iters) *iters = it;
-    if (final_max) *final_max = gmax;
+    if (iters) *iters = std::min(stop, maxit);
+    if (final_max) *final_max = lat->host_result[R_GMAX];
     return TCYM_OK;
 }
 

@@ -49,8 +49,16 @@ struct FmtGroup {
     struct Class {
         StepCoef<double> coef;
         int m0, m1, item0, item1;
+        // persistent launches: groups of members (class-relative first blocks) and the
+        // offsets of the class's schedule and control words in the format's arrays
+        std::vector<int> group_first_block;
+        int sched_off = 0, ctl_off = 0;
     };
     std::vector<Class> classes;
+    std::vector<int> member_block;             // first block of each member (idx order)
+    int *d_sched = nullptr, *d_ctl = nullptr;  // persistent schedules and control words
+    size_t sched_cap = 0, ctl_cap = 0, ctl_used = 0;
+    std::vector<int> h_sched;
 };
 
 int fail(tcym_ctx ctx, cudaError_t e, const char *w) {
@@ -74,6 +82,11 @@ struct tcym_ensemble_s {
     cudaGraphExec_t exec = nullptr;
     int graph_steps = -1;
     bool layout_dirty = true;
+    // K-step persistent launches per coefficient class (k_step_persistent) instead of
+    // one launch per step; group_blocks: blocks per member group (0: one group)
+    bool persistent = false;
+    int group_blocks = 0;
+    std::vector<int> h_ctl;
 };
 
 #define CKE(call)                                                 \
@@ -89,6 +102,7 @@ template <int FMT> static void fill_group(tcym_ensemble ens, FmtGroup &G, int sm
     int blk = 0, red = 0;
     G.general = false;
     G.classes.clear();
+    G.member_block.assign(G.idx.size(), 0);
     for (size_t i = 0; i < G.idx.size(); ++i) {
         const EnsMember &em = ens->members[G.idx[i]];
         const tcym_lattice L = em.lat;
@@ -106,6 +120,7 @@ template <int FMT> static void fill_group(tcym_ensemble ens, FmtGroup &G, int sm
             G.classes.push_back(FmtGroup::Class{cd, (int)i, (int)i, blk, blk});
         m.cur = L->cur;
         m.block_begin = blk;
+        G.member_block[i] = blk;
         m.paired = Fmt<FMT>::PAIRED && L->g.nz % 2 == 0;
         m.tile = m.paired ? tcym_lattice_tile_of(L) : Tile{0, 0, 0, 0, 0, 0};
         if (!m.paired || m.tile.tx != 0) G.general = true;
@@ -151,6 +166,26 @@ static void fill_all(tcym_ensemble ens) {
     }
 }
 
+// Members of each class cut into groups of at least ens->group_blocks blocks (one
+// group when 0); a member is never split.
+static void plan_groups(tcym_ensemble ens, FmtGroup &G) {
+    G.ctl_used = 0;
+    for (FmtGroup::Class &c : G.classes) {
+        c.group_first_block.assign(1, 0);
+        int start = c.item0;
+        for (int i = c.m0; i + 1 < c.m1; ++i) {
+            const int next = G.member_block[i + 1];
+            if (ens->group_blocks > 0 && next - start >= ens->group_blocks) {
+                c.group_first_block.push_back(next - c.item0);
+                start = next;
+            }
+        }
+        c.group_first_block.push_back(c.item1 - c.item0);
+        c.ctl_off = (int)G.ctl_used;
+        G.ctl_used += 2 + (size_t)(c.m1 - c.m0);
+    }
+}
+
 // Sizes the device tables and scratch for the current members and uploads the tables.
 static int upload_tables(tcym_ensemble ens) {
     fill_all(ens);
@@ -158,12 +193,15 @@ static int upload_tables(tcym_ensemble ens) {
     for (int f = 0; f < 4; ++f) {
         FmtGroup &G = ens->groups[f];
         records += (size_t)G.red_total;
+        // device tables grow by doubling: cudaFree synchronises the device, so
+        // members that come and go (the request loop) rarely reallocate
         if (G.h_members.size() > G.d_bytes) {
             cudaFree(G.d_members);
             G.d_members = nullptr;
+            const size_t cap = std::max(G.h_members.size(), 2 * G.d_bytes);
             G.d_bytes = 0;
-            CKE(cudaMalloc(&G.d_members, G.h_members.size()));
-            G.d_bytes = G.h_members.size();
+            CKE(cudaMalloc(&G.d_members, cap));
+            G.d_bytes = cap;
             ens->layout_dirty = true;
         }
         if (!G.h_members.empty())
@@ -173,12 +211,15 @@ static int upload_tables(tcym_ensemble ens) {
     if (records > ens->partial_records) {
         cudaFree(ens->partial);
         ens->partial = nullptr;
+        const size_t cap = std::max(records, 2 * ens->partial_records);
         ens->partial_records = 0;
-        CKE(cudaMalloc(&ens->partial, sizeof(double) * P_WIDTH * records));
-        ens->partial_records = records;
+        CKE(cudaMalloc(&ens->partial, sizeof(double) * P_WIDTH * cap));
+        ens->partial_records = cap;
+        ens->layout_dirty = true;
     }
-    const size_t n = ens->members.size();
-    if (n > ens->reduce_cap) {
+    const size_t n0 = ens->members.size();
+    if (n0 > ens->reduce_cap) {
+        const size_t n = std::max(n0, 2 * ens->reduce_cap);
         cudaFree(ens->d_reduce);
         cudaFree(ens->d_out);
         cudaFreeHost(ens->h_out);
@@ -210,6 +251,69 @@ template <int FMT> static cudaError_t launch_group_step(tcym_ensemble ens, int f
     return LaunchBatch<FMT>::step(table, (int)G.idx.size(), G.total_blocks, k, G.grid, G.general, s);
 }
 
+// Does format f step by persistent K-step launches?
+static bool persistent_format(tcym_ensemble ens, int f) {
+    const FmtGroup &G = ens->groups[f];
+    return ens->persistent && (f == FMT_SU2_F32 || f == FMT_SU3_F32) && !G.general && !G.idx.empty();
+}
+
+// Schedules and control words of the persistent launches for chunks of nsteps
+// (uploaded before the capture, which only refers to them).
+static int prepare_persistent(tcym_ensemble ens, int nsteps) {
+    for (int f = 0; f < 4; ++f) {
+        if (!persistent_format(ens, f)) continue;
+        FmtGroup &G = ens->groups[f];
+        plan_groups(ens, G);
+        G.h_sched.clear();
+        for (FmtGroup::Class &c : G.classes) {
+            c.sched_off = (int)G.h_sched.size();
+            for (int b : c.group_first_block) G.h_sched.push_back(nsteps * b);
+            for (int b : c.group_first_block) G.h_sched.push_back(b);
+        }
+        if (G.h_sched.size() > G.sched_cap) {
+            cudaFree(G.d_sched);
+            G.d_sched = nullptr;
+            const size_t cap = std::max(G.h_sched.size(), 2 * G.sched_cap);
+            G.sched_cap = 0;
+            CKE(cudaMalloc(&G.d_sched, sizeof(int) * cap));
+            G.sched_cap = cap;
+        }
+        CKE(cudaMemcpy(G.d_sched, G.h_sched.data(), sizeof(int) * G.h_sched.size(), cudaMemcpyHostToDevice));
+        if (G.ctl_used > G.ctl_cap) {
+            cudaFree(G.d_ctl);
+            G.d_ctl = nullptr;
+            const size_t cap = std::max(G.ctl_used, 2 * G.ctl_cap);
+            G.ctl_cap = 0;
+            CKE(cudaMalloc(&G.d_ctl, sizeof(int) * cap));
+            G.ctl_cap = cap;
+        }
+    }
+    return TCYM_OK;
+}
+
+// The K steps of format f as one persistent launch per coefficient class (captured).
+template <int FMT> static cudaError_t launch_group_persistent(tcym_ensemble ens, int f, int nsteps, cudaStream_t s) {
+    using T = typename Fmt<FMT>::T;
+    const FmtGroup &G = ens->groups[f];
+    const Member<T> *table = static_cast<const Member<T> *>(G.d_members);
+    cudaError_t e = cudaMemsetAsync(G.d_ctl, 0, sizeof(int) * G.ctl_used, s);
+    const int resident = ens->ctx->sm_count * LaunchBatch<FMT>::persistent_resident_blocks();
+    for (const FmtGroup::Class &c : G.classes) {
+        if (e != cudaSuccess) break;
+        const int ng = (int)c.group_first_block.size() - 1;
+        // each wait gives up after ~1 s at the GB300's 2 GHz clock
+        const PersistentPlan plan{G.d_sched + c.sched_off, ng, nsteps, c.item0, c.item1, 2000000000LL};
+        const int items = nsteps * (c.item1 - c.item0);
+        e = LaunchBatch<FMT>::step_persistent(table, c.m0, c.m1 - c.m0, plan, c.coef, G.d_ctl + c.ctl_off,
+                                              std::max(1, std::min(resident, items)), s);
+    }
+    return e;
+}
+static cudaError_t group_persistent(tcym_ensemble ens, int f, int nsteps, cudaStream_t s) {
+    if (f == FMT_SU2_F32) return launch_group_persistent<FMT_SU2_F32>(ens, f, nsteps, s);
+    return launch_group_persistent<FMT_SU3_F32>(ens, f, nsteps, s);
+}
+
 static cudaError_t group_step(tcym_ensemble ens, int f, int k, cudaStream_t s) {
     switch (f) {
         case FMT_SU2_F32: return launch_group_step<FMT_SU2_F32>(ens, f, k, s);
@@ -226,13 +330,19 @@ static int capture(tcym_ensemble ens, int nsteps) {
         ens->exec = nullptr;
     }
     cudaGraph_t graph = nullptr;
+    int r = prepare_persistent(ens, nsteps);
+    if (r) return r;
     CKE(cudaStreamBeginCapture(ens->st[0], cudaStreamCaptureModeThreadLocal));
     cudaError_t err = cudaEventRecord(ens->fork, ens->st[0]);
     for (int f = 0; f < 4 && err == cudaSuccess; ++f) {
         if (ens->groups[f].idx.empty()) continue;
         cudaStream_t s = ens->st[f];
         if (f != 0) err = cudaStreamWaitEvent(s, ens->fork, 0);
-        for (int k = 0; k < nsteps && err == cudaSuccess; ++k) err = group_step(ens, f, k, s);
+        if (persistent_format(ens, f)) {
+            if (err == cudaSuccess) err = group_persistent(ens, f, nsteps, s);
+        } else {
+            for (int k = 0; k < nsteps && err == cudaSuccess; ++k) err = group_step(ens, f, k, s);
+        }
         if (f != 0 && err == cudaSuccess) {
             err = cudaEventRecord(ens->join[f], s);
             if (err == cudaSuccess) err = cudaStreamWaitEvent(ens->st[0], ens->join[f], 0);
@@ -259,8 +369,12 @@ extern "C" int tcym_ensemble_create(tcym_ctx ctx, tcym_ensemble *out) {
     if (!ens) return TCYM_ERR_OOM;
     ens->ctx = ctx;
     cudaSetDevice(ctx->device);
-    cudaError_t e = cudaSuccess;
-    for (int i = 0; i < 4 && e == cudaSuccess; ++i) e = cudaStreamCreateWithFlags(&ens->st[i], cudaStreamNonBlocking);
+    // the ensemble's streams take the device's highest priority: work queued beside
+    // them (a request being prepared in the request loop) fills the SMs they leave
+    int lo = 0, hi = 0;
+    cudaError_t e = cudaDeviceGetStreamPriorityRange(&lo, &hi);
+    for (int i = 0; i < 4 && e == cudaSuccess; ++i)
+        e = cudaStreamCreateWithPriority(&ens->st[i], cudaStreamNonBlocking, hi);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ens->fork, cudaEventDisableTiming);
     for (int i = 0; i < 4 && e == cudaSuccess; ++i) e = cudaEventCreateWithFlags(&ens->join[i], cudaEventDisableTiming);
     if (e != cudaSuccess) {
@@ -278,7 +392,11 @@ extern "C" int tcym_ensemble_destroy(tcym_ensemble ens) {
     for (int i = 0; i < 4; ++i)
         if (ens->st[i]) cudaStreamSynchronize(ens->st[i]);
     if (ens->exec) cudaGraphExecDestroy(ens->exec);
-    for (int f = 0; f < 4; ++f) cudaFree(ens->groups[f].d_members);
+    for (int f = 0; f < 4; ++f) {
+        cudaFree(ens->groups[f].d_members);
+        cudaFree(ens->groups[f].d_sched);
+        cudaFree(ens->groups[f].d_ctl);
+    }
     cudaFree(ens->partial);
     cudaFree(ens->d_reduce);
     cudaFree(ens->d_out);
@@ -310,6 +428,14 @@ extern "C" int tcym_ensemble_add(tcym_ensemble ens, tcym_lattice lat, int dynami
     return TCYM_OK;
 }
 
+extern "C" int tcym_ensemble_set_persistent(tcym_ensemble ens, int group_blocks) {
+    if (!ens) return TCYM_ERR_ARG;
+    ens->persistent = group_blocks >= 0;
+    ens->group_blocks = group_blocks > 0 ? group_blocks : 0;
+    ens->layout_dirty = true;
+    return TCYM_OK;
+}
+
 extern "C" int tcym_ensemble_remove(tcym_ensemble ens, tcym_lattice lat) {
     if (!ens || !lat) return TCYM_ERR_ARG;
     auto it = std::find_if(ens->members.begin(), ens->members.end(), [&](const EnsMember &m) { return m.lat == lat; });
@@ -335,6 +461,21 @@ extern "C" int tcym_ensemble_step(tcym_ensemble ens, int nsteps) {
     if (ens->layout_dirty || !ens->exec || ens->graph_steps != nsteps)
         if ((r = capture(ens, nsteps))) return r;
     CKE(cudaGraphLaunch(ens->exec, ens->st[0]));
+    // a persistent launch that gave up waiting raised its error word
+    for (int f = 0; f < 4; ++f) {
+        if (!persistent_format(ens, f)) continue;
+        FmtGroup &G = ens->groups[f];
+        ens->h_ctl.resize(G.ctl_used);
+        CKE(cudaMemcpyAsync(ens->h_ctl.data(), G.d_ctl, sizeof(int) * G.ctl_used, cudaMemcpyDeviceToHost,
+                            ens->st[0]));
+        CKE(cudaStreamSynchronize(ens->st[0]));
+        for (const FmtGroup::Class &c : G.classes)
+            if (ens->h_ctl[c.ctl_off + 1]) {
+                tcym_set_error(ens->ctx, "tcym_ensemble_step: a persistent launch timed out waiting for a member's "
+                                         "previous step");
+                return TCYM_ERR_TIMEOUT;
+            }
+    }
     // bookkeeping of every member; periodic FP64 reunitarisation of FP32 links
     for (EnsMember &m : ens->members) {
         tcym_lattice L = m.lat;

@@ -61,16 +61,18 @@ template <int FMT> struct H {
                         int64_t p;
                         bool seam;
                         if (!tile_pair(g, t, b, tid, p, seam)) continue;
-                        if (seam) site_step_pair<F, true>(g, Uin, Uout, E, c, p);
-                        else site_step_pair<F, false>(g, Uin, Uout, E, c, p);
+                        f2 sm[3 * F::NA];
+                        if (seam) site_step_pair<F, true>(g, Uin, Uout, E, c, p, 0, sm, 1);
+                        else site_step_pair<F, false>(g, Uin, Uout, E, c, p, 0, sm, 1);
                     }
                 return;
             }
         }
         for (int64_t s = 0; s < g.V; ++s) {
-            if (doE && doU) site_step<F, true, true>(g, Uin, Uout, E, c, s);
-            else if (doE) site_step<F, true, false>(g, Uin, Uout, E, c, s);
-            else site_step<F, false, true>(g, Uin, Uout, E, c, s);
+            T sm[3 * F::NA];
+            if (doE && doU) site_step<F, true, true>(g, Uin, Uout, E, c, s, 0, sm, 1);
+            else if (doE) site_step<F, true, false>(g, Uin, Uout, E, c, s, 0, sm, 1);
+            else site_step<F, false, true>(g, Uin, Uout, E, c, s, 0, sm, 1);
         }
     }
     // one fused step of the storage indices [i0, i1) as Launch::step_range runs it: the
@@ -86,13 +88,17 @@ template <int FMT> struct H {
                         int64_t p;
                         bool seam;
                         if (!tile_pair(g, t, b, tid, p, seam)) continue;
-                        if (seam) site_step_pair<F, true>(g, Uin, Uout, E, c, p);
-                        else site_step_pair<F, false>(g, Uin, Uout, E, c, p);
+                        f2 sm[3 * F::NA];
+                        if (seam) site_step_pair<F, true>(g, Uin, Uout, E, c, p, 0, sm, 1);
+                        else site_step_pair<F, false>(g, Uin, Uout, E, c, p, 0, sm, 1);
                     }
                 return;
             }
         }
-        for (int64_t s = i0; s < i1; ++s) site_step<F, true, true>(g, Uin, Uout, E, c, s);
+        for (int64_t s = i0; s < i1; ++s) {
+            T sm[3 * F::NA];
+            site_step<F, true, true>(g, Uin, Uout, E, c, s, 0, sm, 1);
+        }
     }
     static void flow_cb(const Geom &g, void *U, double dtau, int nsweeps) {
         const T fc[3] = {T(-2), T(-2), T(-2)}, cn[3] = {T(1), T(1), T(1)}, uc[3] = {T(-dtau), T(-dtau), T(-dtau)};

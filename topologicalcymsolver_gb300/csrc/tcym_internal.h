@@ -57,6 +57,10 @@ struct tcym_lattice_s {
     // the first step it has not drawn yet (kept so a snapshot can resume the stream)
     uint64_t noise_seed = 0, noise_next = 0;
     bool noise_valid = false;
+    // device memory from a stream-ordered pool (cudaMallocFromPoolAsync / cudaFreeAsync
+    // on the lattice's stream): creating and destroying such a lattice never waits for
+    // the rest of the device (the request loop's lattices); nullptr: cudaMalloc
+    cudaMemPool_t pool = nullptr;
     tcym::Tile tile{};   // block tiling of the paired step
     bool tile_chosen = false;
     cudaStream_t side[2] = {nullptr, nullptr};  // pipelined host transfers (created with the staging)
@@ -88,6 +92,13 @@ tcym::StepCoef<double> tcym_coef(const double *a, int mode, double dt, double ga
 int tcym_reduce(tcym_lattice lat, int mask, double ncs_dt);
 // frees the Gauss-restore and AoS staging scratch of a lattice (reallocated on next use)
 void tcym_lattice_release_scratch(tcym_lattice lat);
+// a lattice whose device memory comes from `pool` on its own stream (see tcym_lattice_s::pool);
+// its host result block is pageable, so neither creation nor destruction synchronises the device
+int tcym_lattice_create_pooled(tcym_ctx ctx, int nc, int nx, int ny, int nz, int precision, cudaMemPool_t pool,
+                               tcym_lattice *out);
+// device allocation and release for a lattice: from its pool when it has one
+cudaError_t tcym_lattice_alloc(tcym_lattice lat, void **p, size_t bytes);
+void tcym_lattice_free_mem(tcym_lattice lat, void *p);
 // the block tiling of lat's paired step, autotuned on first use (tcym_autotune.cu)
 const tcym::Tile &tcym_lattice_tile_of(tcym_lattice lat);
 int tcym_run_steps(tcym_lattice lat, int mode, double dt, double gamma, double T, uint64_t seed, uint64_t step0,

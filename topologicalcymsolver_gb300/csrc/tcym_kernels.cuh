@@ -50,8 +50,10 @@ constexpr int kThreadsPair = 128;
 #ifndef TCYM_PAIR_SEAM_SPLIT
 #define TCYM_PAIR_SEAM_SPLIT 1
 #endif
+// SU(3): 4 blocks (128 registers, no spills) measured 0.331 ms per 128^3 step
+// against 0.342 ms at 3 (166 registers)
 #ifndef TCYM_SU3_PAIR_MINBLOCKS
-#define TCYM_SU3_PAIR_MINBLOCKS 3
+#define TCYM_SU3_PAIR_MINBLOCKS 4
 #endif
 // SU(2): 7 blocks (72 registers, a 4-byte spill) measured 0.090 ms per 128^3
 // step against 0.094 ms at 6 (80 registers) and 0.107 ms at 5 (96, no spill)
@@ -81,12 +83,17 @@ template <class T> StepCoef<T> coef_cast(const StepCoef<double> &c) {
 
 // ------------------------------------------------------------------ kernels
 // sites [s0, s1)
+// shared-memory slots of the plaquette projections (site_step, site_step_pair)
+template <int FMT> constexpr int plaq_slots() { return 3 * Fmt<FMT>::NA; }
+
 template <int FMT, bool DO_E, bool DO_U>
 __global__ void __launch_bounds__(threads_for<FMT>(), min_blocks_for<FMT>()) k_step(Geom g, const void *Uin, void *Uout, void *E,
                                                              StepCoef<typename Fmt<FMT>::T> c, int64_t s0, int64_t s1) {
+    using T = typename Fmt<FMT>::T;
+    __shared__ T sm[DO_E ? plaq_slots<FMT>() * threads_for<FMT>() : 1];
     const int64_t s = s0 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= s1) return;
-    site_step<Fmt<FMT>, DO_E, DO_U>(g, Uin, Uout, E, c, s);
+    site_step<Fmt<FMT>, DO_E, DO_U>(g, Uin, Uout, E, c, s, 0, sm + threadIdx.x, threads_for<FMT>());
 }
 
 // one thread per site pair (FP32 formats, even nz); blocks touching the seam
@@ -96,6 +103,7 @@ __global__ void __launch_bounds__(threads_for<FMT>(), min_blocks_for<FMT>()) k_s
 template <int FMT, bool TILED>
 __global__ void __launch_bounds__(kThreadsPair, pair_min_blocks_for<FMT>())
     k_step_pair(Geom g, const void *Uin, void *Uout, void *E, StepCoef<float> c, Tile t) {
+    __shared__ f2 sm[plaq_slots<FMT>() * kThreadsPair];
     int64_t p;
     bool seam;
     if constexpr (TILED) {
@@ -107,10 +115,10 @@ __global__ void __launch_bounds__(kThreadsPair, pair_min_blocks_for<FMT>())
         seam = pairs_touch_seam(g, p0, kThreadsPair);
     }
 #if TCYM_PAIR_SEAM_SPLIT
-    if (seam) site_step_pair<Fmt<FMT>, true>(g, Uin, Uout, E, c, p);
-    else site_step_pair<Fmt<FMT>, false>(g, Uin, Uout, E, c, p);
+    if (seam) site_step_pair<Fmt<FMT>, true>(g, Uin, Uout, E, c, p, 0, sm + threadIdx.x, kThreadsPair);
+    else site_step_pair<Fmt<FMT>, false>(g, Uin, Uout, E, c, p, 0, sm + threadIdx.x, kThreadsPair);
 #else
-    site_step_pair<Fmt<FMT>, true>(g, Uin, Uout, E, c, p);
+    site_step_pair<Fmt<FMT>, true>(g, Uin, Uout, E, c, p, 0, sm + threadIdx.x, kThreadsPair);
 #endif
 }
 
@@ -190,8 +198,8 @@ __global__ void __launch_bounds__(kRedThreads) k_observables(Geom g, const void 
 
 // Gauss violation into the FP64 scratch G[a*V + s]; partial maxima as for observables.
 template <int FMT>
-__global__ void __launch_bounds__(kRedThreads) k_gauss_compute(Geom g, const void *U, const void *E, double *G,
-                                                               double *partial) {
+__device__ __forceinline__ void gauss_compute_block(const Geom &g, const void *U, const void *E, double *G,
+                                                    double *partial) {
     using F = Fmt<FMT>;
     double v[P_WIDTH];
 #pragma unroll
@@ -208,10 +216,34 @@ __global__ void __launch_bounds__(kRedThreads) k_gauss_compute(Geom g, const voi
     }
     block_partial(v, partial);
 }
+template <int FMT>
+__global__ void __launch_bounds__(kRedThreads) k_gauss_compute(Geom g, const void *U, const void *E, double *G,
+                                                               double *partial) {
+    gauss_compute_block<FMT>(g, U, E, G, partial);
+}
 
 template <int FMT>
 __global__ void __launch_bounds__(threads_for<FMT>()) k_gauss_update(Geom g, const void *U, void *E, const double *G,
                                                                      double gam) {
+    int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= g.V) return;
+    site_gauss_update<Fmt<FMT>>(g, U, E, G, gam, s);
+}
+
+// The same two kernels for iteration `it` of a restore whose control block
+// holds, in ctl[0], the first iteration that is not to run (the finaliser of the
+// deciding reduction lowers it): a kernel of a later iteration returns at once,
+// so the host can queue many iterations between its checks.
+template <int FMT>
+__global__ void __launch_bounds__(kRedThreads) k_gauss_compute_it(Geom g, const void *U, const void *E, double *G,
+                                                                  double *partial, const double *ctl, int it) {
+    if ((double)it >= ctl[0]) return;  // the same value for every thread of the grid
+    gauss_compute_block<FMT>(g, U, E, G, partial);
+}
+template <int FMT>
+__global__ void __launch_bounds__(threads_for<FMT>()) k_gauss_update_it(Geom g, const void *U, void *E, const double *G,
+                                                                        double gam, const double *ctl, int it) {
+    if ((double)it >= ctl[0]) return;
     int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= g.V) return;
     site_gauss_update<Fmt<FMT>>(g, U, E, G, gam, s);
@@ -358,6 +390,16 @@ template <int FMT> struct Launch {
         k_gauss_update<FMT><<<grid_for(g.V, TPB), TPB, 0, st>>>(g, U, E, G, gam);
         return cudaGetLastError();
     }
+    static cudaError_t gauss_compute_it(const Geom &g, const void *U, const void *E, double *G, double *partial,
+                                        int blocks, const double *ctl, int it, cudaStream_t st) {
+        k_gauss_compute_it<FMT><<<blocks, kRedThreads, 0, st>>>(g, U, E, G, partial, ctl, it);
+        return cudaGetLastError();
+    }
+    static cudaError_t gauss_update_it(const Geom &g, const void *U, void *E, const double *G, double gam,
+                                       const double *ctl, int it, cudaStream_t st) {
+        k_gauss_update_it<FMT><<<grid_for(g.V, TPB), TPB, 0, st>>>(g, U, E, G, gam, ctl, it);
+        return cudaGetLastError();
+    }
     static cudaError_t set_zero(const Geom &g, void *U, void *E, cudaStream_t st) {
         k_set_zero<FMT><<<grid_for(g.V, 256), 256, 0, st>>>(g, U, E);
         return cudaGetLastError();
@@ -406,5 +448,11 @@ cudaError_t finalize_obs(const double *partial, int blocks, int na, int64_t V, d
                          cudaStream_t st);
 // loads k_finalize's code now (with lazy module loading it would load at its first launch)
 cudaError_t preload_finalize();
+// The finaliser of a Gauss restore's reduction in iteration `it` (-1: the initial
+// deviation), skipped when it >= ctl[0].  A non-finite reduction sets ctl[1] and
+// stops the restore after this iteration; with `check` (the deviation the
+// reference tests, GaussRestore.cpp:150), a signed maximum <= tol stops it too.
+cudaError_t finalize_restore(const double *partial, int blocks, int na, int64_t V, double *result, double *ctl,
+                             double tol, int it, bool check, cudaStream_t st);
 
 }  // namespace tcym

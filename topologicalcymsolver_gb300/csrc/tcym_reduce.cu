@@ -59,6 +59,25 @@ __global__ void __launch_bounds__(kRedThreads) k_finalize(const double *partial,
     finalize_block(partial, blocks, na, V, ncs_dt, res, nullptr, nullptr);
 }
 
+__global__ void __launch_bounds__(kRedThreads) k_finalize_restore(const double *partial, int blocks, int na,
+                                                                  int64_t V, double *res, double *ctl, double tol,
+                                                                  int it, int check) {
+    if ((double)it >= ctl[0]) return;  // the same value for every thread
+    finalize_block(partial, blocks, na, V, 0.0, res, nullptr, nullptr);
+    if (threadIdx.x == 0) {
+        const double gmax = res[R_GMAX];
+        const bool bad = res[R_NONFINITE] != 0.0 || !(gmax == gmax);
+        if (bad) ctl[1] = 1.0;
+        if (bad || (check && gmax <= tol)) ctl[0] = fmin(ctl[0], (double)(it + 1));
+    }
+}
+
+cudaError_t finalize_restore(const double *partial, int blocks, int na, int64_t V, double *result, double *ctl,
+                             double tol, int it, bool check, cudaStream_t st) {
+    k_finalize_restore<<<1, kRedThreads, 0, st>>>(partial, blocks, na, V, result, ctl, tol, it, check ? 1 : 0);
+    return cudaGetLastError();
+}
+
 cudaError_t preload_finalize() {
     cudaFuncAttributes fa;
     return cudaFuncGetAttributes(&fa, k_finalize);

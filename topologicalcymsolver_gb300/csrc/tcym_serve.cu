@@ -1,11 +1,25 @@
 // Serving loop: continuous batching of independent trajectory requests.
 //
 // The reference runs one trajectory per process and seed (SU2Solver.cpp:148-169,
-// SphaleronSimulation.cpp:571-616).  Here a background thread owns an
-// ensemble; requests are admitted in arrival order while the device-memory
-// budget and the slot limit allow, stepped together, sampled every `stride`
-// steps (N_CS time series) and retired as soon as they finish, which frees
-// their memory for the next arrivals.  Every wait has a time limit.
+// SphaleronSimulation.cpp:571-616).  Here two kinds of host threads share one
+// GPU:
+//
+//   * preparer threads take requests in arrival order while the device-memory
+//     budget and the slot limit allow, and build each one's initial state on the
+//     request's own stream: U = 1, E ~ N(0, T) from the request's Philox field
+//     stream, Gauss-restored in FP64 (a temporary FP64 lattice for FP32 requests,
+//     copied into FP32 storage) -- the restore queues its iterations in batches
+//     and learns of convergence from a device-side flag;
+//   * the tick thread owns the running ensemble: at each tick boundary it joins
+//     the prepared requests, advances every running request `stride` steps in
+//     the ensemble's batched launches, appends (steps, N_CS) per request and
+//     retires the finished ones, which frees their memory for the next arrivals.
+//
+// So a tick never waits for a preparation: their kernels share the device (the
+// ensemble's streams have the higher priority), and the request lattices take
+// their memory from a stream-ordered pool, whose allocations and releases do
+// not synchronise the device the way cudaMalloc and cudaFree do.  Every wait
+// has a time limit.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -25,26 +39,42 @@
 namespace {
 
 using Clock = std::chrono::steady_clock;
+constexpr int kPreparers = 2;         // preparation threads
+constexpr size_t kTickRecord = 8192;  // tick records kept for tcym_server_ticks
 
 struct Req {
     tcym_request spec;
     int status = TCYM_REQ_QUEUED;
     int steps_done = 0;
     int target = 0;                 // steps rounded up to a multiple of the stride
-    size_t footprint = 0;
+    size_t footprint = 0;           // device bytes while running
+    size_t prep_extra = 0;          // device bytes held only while it is prepared
     tcym_lattice lat = nullptr;
     std::vector<double> series;     // (steps, N_CS) pairs
     Clock::time_point submitted, finished;
     int error = TCYM_OK;
 };
 
-size_t footprint_of(const tcym_request &r, int sm_count) {
+size_t reduction_bytes(size_t V, int sm_count) {
+    return sizeof(double) * (12 * (size_t)sm_count * 8 + 16) + 8 * 32 * ((V + 255) / 256);
+}
+// links (ping-pong) + fields + reductions of a lattice in `fmt`
+size_t lattice_bytes(int fmt, size_t V, int sm_count) {
+    const size_t nst = tcym_stored_sites(fmt, (int64_t)V);
+    return 2 * 3 * tcym_link_bytes(fmt) * nst + 3 * tcym_field_bytes(fmt) * nst + reduction_bytes(V, sm_count);
+}
+
+void footprint_of(const tcym_request &r, int sm_count, size_t &running, size_t &extra) {
     const int fmt = tcym_format_of(r.nc, r.precision);
     const size_t V = (size_t)r.L * r.L * r.L;
-    const size_t na = r.nc == 2 ? 3 : 8;
-    const size_t nst = tcym_stored_sites(fmt, (int64_t)V);
-    return 2 * 3 * tcym_link_bytes(fmt) * nst + 3 * tcym_field_bytes(fmt) * nst + sizeof(double) * na * V  // restore scratch
-           + sizeof(double) * (12 * (size_t)sm_count * 8 + 16) + 8 * 32 * ((V + 255) / 256);                  // reductions
+    const size_t na = r.nc == 2 ? 3 : 8, nmd = r.nc == 2 ? 4 : 18;
+    running = lattice_bytes(fmt, V, sm_count);
+    // the FP64 preparation lattice with its restore scratch; FP32 requests also
+    // stage the FP64 state (AoS) for the conversion into FP32 storage
+    const int fmt64 = tcym_format_of(r.nc, TCYM_FP64);
+    extra = sizeof(double) * (na * V + 4);
+    if (r.precision != TCYM_FP64)
+        extra += lattice_bytes(fmt64, V, sm_count) + sizeof(double) * 3 * (nmd + na) * V;
 }
 
 }  // namespace
@@ -54,40 +84,56 @@ struct tcym_server_s {
     size_t budget = 0, used = 0;
     int max_active = 0, stride = 20;
     std::mutex mu;
-    std::condition_variable cv;       // submissions / stop
+    std::condition_variable cv;       // work for the tick thread / stop
+    std::condition_variable prep_cv;  // work for the preparers / stop
     std::condition_variable done_cv;  // completions
-    std::deque<uint64_t> queue;
+    std::deque<uint64_t> queue;       // submitted, not yet taken by a preparer
+    std::deque<uint64_t> ready;       // prepared, not yet in the ensemble
     std::map<uint64_t, Req> reqs;
     std::vector<uint64_t> active;     // in ensemble order
+    int preparing = 0;
     uint64_t next_id = 1;
     tcym_ensemble ens = nullptr;
-    std::thread worker;
+    cudaMemPool_t pool = nullptr;
+    std::thread ticker;
+    std::thread preparers[kPreparers];
     bool stop = false;
     double link_updates = 0.0;
-    uint64_t completed = 0, failed = 0;
+    uint64_t completed = 0, failed = 0, ticks = 0;
+    double prep_seconds = 0.0;
+    std::vector<double> tick_ms, tick_prep;  // per tick: duration, preparations under way at its start
     int loop_error = TCYM_OK;
 };
 
 namespace {
 
 // Initial state of a request: U = 1, E ~ N(0, T) per component (Philox field
-// stream of the request's seed), Gauss-restored; the restore scratch is freed.
+// stream of the request's seed), Gauss-restored in FP64 to 1e-12 (at most 400
+// iterations), in the request's storage; temporary memory is released.
 int prepare(tcym_server srv, Req &r) {
     const tcym_request &q = r.spec;
-    int rc = tcym_lattice_create(srv->ctx, q.nc, q.L, q.L, q.L, q.precision, &r.lat);
-    if (rc) return rc;
-    if ((rc = tcym_set_zero(r.lat))) return rc;
-    if ((rc = tcym_gaussian_efield(r.lat, std::sqrt(q.T), q.seed))) return rc;
-    const double tol = q.precision == TCYM_FP64 ? 1e-12 : 1e-6;
-    if ((rc = tcym_gauss_restore(r.lat, tol, 400, nullptr, nullptr))) return rc;
-    tcym_lattice_release_scratch(r.lat);
-    return tcym_ensemble_add(srv->ens, r.lat, q.dynamics, q.dt, q.gamma, q.T, q.seed, 0);
+    tcym_lattice ic = nullptr;
+    int rc = tcym_lattice_create_pooled(srv->ctx, q.nc, q.L, q.L, q.L, TCYM_FP64, srv->pool, &ic);
+    if (!rc) rc = tcym_set_zero(ic);
+    if (!rc) rc = tcym_gaussian_efield(ic, std::sqrt(q.T), q.seed);
+    if (!rc) rc = tcym_gauss_restore(ic, 1e-12, 400, nullptr, nullptr);
+    if (!rc && q.precision == TCYM_FP64) {
+        tcym_lattice_release_scratch(ic);
+        r.lat = ic;
+        return TCYM_OK;
+    }
+    if (!rc) rc = tcym_lattice_create_pooled(srv->ctx, q.nc, q.L, q.L, q.L, q.precision, srv->pool, &r.lat);
+    if (!rc) rc = tcym_lattice_copy(r.lat, ic);
+    if (ic) tcym_lattice_destroy(ic);
+    if (!rc) tcym_lattice_release_scratch(r.lat);
+    return rc;
 }
 
-void retire(tcym_server srv, Req &r, int status) {
+// joined: the request is an ensemble member (only the tick thread touches the ensemble)
+void retire(tcym_server srv, Req &r, int status, bool joined) {
     if (r.lat) {
-        tcym_ensemble_remove(srv->ens, r.lat);
-        tcym_lattice_destroy(r.lat);
+        if (joined) tcym_ensemble_remove(srv->ens, r.lat);
+        tcym_lattice_destroy(r.lat);  // pooled: releases without a device synchronisation
         r.lat = nullptr;
     }
     srv->used -= r.footprint;
@@ -96,23 +142,58 @@ void retire(tcym_server srv, Req &r, int status) {
     if (status == TCYM_REQ_DONE) ++srv->completed; else ++srv->failed;
 }
 
-void loop(tcym_server srv) {
+void prepare_loop(tcym_server srv) {
     cudaSetDevice(srv->ctx->device);
     std::unique_lock<std::mutex> lk(srv->mu);
     while (!srv->stop) {
-        // admission, in arrival order, while memory and slots allow
-        while (!srv->queue.empty() && (int)srv->active.size() < srv->max_active) {
-            Req &r = srv->reqs[srv->queue.front()];
-            if (srv->used + r.footprint > srv->budget) break;
-            const uint64_t id = srv->queue.front();
-            srv->queue.pop_front();
-            srv->used += r.footprint;
-            lk.unlock();
-            int rc = prepare(srv, r);
-            lk.lock();
+        const int slots = (int)srv->active.size() + (int)srv->ready.size() + srv->preparing;
+        if (srv->queue.empty() || slots >= srv->max_active) {
+            srv->prep_cv.wait_for(lk, std::chrono::milliseconds(50));
+            continue;
+        }
+        const uint64_t id = srv->queue.front();
+        Req &r = srv->reqs[id];
+        if (srv->used + r.footprint + r.prep_extra > srv->budget) {  // in arrival order: wait for memory
+            srv->prep_cv.wait_for(lk, std::chrono::milliseconds(50));
+            continue;
+        }
+        srv->queue.pop_front();
+        srv->used += r.footprint + r.prep_extra;
+        ++srv->preparing;
+        lk.unlock();
+        const auto t0 = Clock::now();
+        const int rc = prepare(srv, r);
+        const double secs = std::chrono::duration<double>(Clock::now() - t0).count();
+        lk.lock();
+        srv->prep_seconds += secs;
+        srv->used -= r.prep_extra;
+        --srv->preparing;
+        if (rc) {
+            r.error = rc;
+            retire(srv, r, TCYM_REQ_FAILED, false);
+            srv->done_cv.notify_all();
+        } else {
+            srv->ready.push_back(id);
+            srv->cv.notify_all();
+        }
+        srv->prep_cv.notify_all();
+    }
+}
+
+void tick_loop(tcym_server srv) {
+    cudaSetDevice(srv->ctx->device);
+    std::unique_lock<std::mutex> lk(srv->mu);
+    while (!srv->stop) {
+        // prepared requests join at the tick boundary
+        while (!srv->ready.empty()) {
+            const uint64_t id = srv->ready.front();
+            srv->ready.pop_front();
+            Req &r = srv->reqs[id];
+            const tcym_request &q = r.spec;
+            const int rc = tcym_ensemble_add(srv->ens, r.lat, q.dynamics, q.dt, q.gamma, q.T, q.seed, 0);
             if (rc) {
                 r.error = rc;
-                retire(srv, r, TCYM_REQ_FAILED);
+                retire(srv, r, TCYM_REQ_FAILED, false);
                 srv->done_cv.notify_all();
                 continue;
             }
@@ -120,20 +201,32 @@ void loop(tcym_server srv) {
             srv->active.push_back(id);
         }
         if (srv->active.empty()) {
-            srv->cv.wait_for(lk, std::chrono::milliseconds(50));
+            srv->cv.wait_for(lk, std::chrono::milliseconds(20));
             continue;
         }
         // one tick: every active request advances `stride` steps and is sampled
         const int n = (int)srv->active.size();
+        const int preparing = srv->preparing;
         std::vector<double> ncs(n), edb(n);
         lk.unlock();
+        const auto t0 = Clock::now();
         int rc = tcym_ensemble_step(srv->ens, srv->stride);
         if (!rc) rc = tcym_ensemble_measure(srv->ens, srv->stride, edb.data(), ncs.data());
+        const double ms = std::chrono::duration<double, std::milli>(Clock::now() - t0).count();
         lk.lock();
+        ++srv->ticks;
+        if (srv->tick_ms.size() >= kTickRecord) {
+            srv->tick_ms.erase(srv->tick_ms.begin(), srv->tick_ms.begin() + kTickRecord / 2);
+            srv->tick_prep.erase(srv->tick_prep.begin(), srv->tick_prep.begin() + kTickRecord / 2);
+        }
+        srv->tick_ms.push_back(ms);
+        srv->tick_prep.push_back((double)preparing);
         if (rc) {  // a device failure ends the loop; every pending request fails
             srv->loop_error = rc;
-            for (uint64_t id : srv->active) retire(srv, srv->reqs[id], TCYM_REQ_FAILED);
+            for (uint64_t id : srv->active) retire(srv, srv->reqs[id], TCYM_REQ_FAILED, true);
             srv->active.clear();
+            srv->stop = true;
+            srv->prep_cv.notify_all();
             srv->done_cv.notify_all();
             break;
         }
@@ -146,14 +239,17 @@ void loop(tcym_server srv) {
             r.series.push_back(ncs[i]);
             if (!std::isfinite(edb[i]) || !std::isfinite(ncs[i])) {  // health check: non-finite state
                 r.error = TCYM_ERR_NONFINITE;
-                retire(srv, r, TCYM_REQ_FAILED);
+                retire(srv, r, TCYM_REQ_FAILED, true);
             } else if (r.steps_done >= r.target) {
-                retire(srv, r, TCYM_REQ_DONE);
+                retire(srv, r, TCYM_REQ_DONE, true);
             } else {
                 still.push_back(srv->active[i]);
             }
         }
-        if (still.size() != srv->active.size()) srv->done_cv.notify_all();
+        if (still.size() != srv->active.size()) {
+            srv->done_cv.notify_all();
+            srv->prep_cv.notify_all();  // memory and slots were freed
+        }
         srv->active.swap(still);
     }
 }
@@ -170,12 +266,32 @@ extern "C" int tcym_server_create(tcym_ctx ctx, size_t hbm_budget_bytes, int max
     srv->budget = hbm_budget_bytes;
     srv->max_active = max_active;
     srv->stride = stride;
+    cudaSetDevice(ctx->device);
+    // the request lattices' pool keeps up to the budget in reserve once used, so
+    // later requests reuse memory without going back to the driver
+    cudaMemPoolProps props = {};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = ctx->device;
+    cudaError_t e = cudaMemPoolCreate(&srv->pool, &props);
+    if (e == cudaSuccess) {
+        uint64_t keep = hbm_budget_bytes;
+        e = cudaMemPoolSetAttribute(srv->pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+    if (e != cudaSuccess) {
+        tcym_set_error(ctx, "tcym_server_create: memory pool: %s", cudaGetErrorString(e));
+        if (srv->pool) cudaMemPoolDestroy(srv->pool);
+        delete srv;
+        return TCYM_ERR_CUDA;
+    }
     int rc = tcym_ensemble_create(ctx, &srv->ens);
     if (rc) {
+        cudaMemPoolDestroy(srv->pool);
         delete srv;
         return rc;
     }
-    srv->worker = std::thread(loop, srv);
+    srv->ticker = std::thread(tick_loop, srv);
+    for (auto &t : srv->preparers) t = std::thread(prepare_loop, srv);
     *out = srv;
     return TCYM_OK;
 }
@@ -187,10 +303,16 @@ extern "C" int tcym_server_destroy(tcym_server srv) {
         srv->stop = true;
     }
     srv->cv.notify_all();
-    if (srv->worker.joinable()) srv->worker.join();
+    srv->prep_cv.notify_all();
+    if (srv->ticker.joinable()) srv->ticker.join();
+    for (auto &t : srv->preparers)
+        if (t.joinable()) t.join();
+    tcym_ensemble_destroy(srv->ens);
     for (auto &kv : srv->reqs)
         if (kv.second.lat) tcym_lattice_destroy(kv.second.lat);
-    tcym_ensemble_destroy(srv->ens);
+    cudaSetDevice(srv->ctx->device);
+    cudaDeviceSynchronize();  // the pooled releases, before the pool goes
+    cudaMemPoolDestroy(srv->pool);
     delete srv;
     return TCYM_OK;
 }
@@ -204,10 +326,12 @@ extern "C" int tcym_server_submit(tcym_server srv, const tcym_request *req, uint
         return TCYM_ERR_ARG;
     Req r;
     r.spec = q;
-    r.footprint = footprint_of(q, srv->ctx->sm_count);
-    if (r.footprint > srv->budget) {
-        tcym_set_error(srv->ctx, "tcym_server_submit: the request needs %zu bytes, more than the budget %zu",
-                       r.footprint, srv->budget);
+    footprint_of(q, srv->ctx->sm_count, r.footprint, r.prep_extra);
+    if (r.footprint + r.prep_extra > srv->budget) {
+        tcym_set_error(srv->ctx,
+                       "tcym_server_submit: the request needs %zu bytes (%zu while it is prepared), more than the "
+                       "budget %zu",
+                       r.footprint, r.footprint + r.prep_extra, srv->budget);
         return TCYM_ERR_ADMISSION;
     }
     r.target = ((q.nsteps + srv->stride - 1) / srv->stride) * srv->stride;
@@ -219,7 +343,7 @@ extern "C" int tcym_server_submit(tcym_server srv, const tcym_request *req, uint
         srv->reqs.emplace(*id, std::move(r));
         srv->queue.push_back(*id);
     }
-    srv->cv.notify_all();
+    srv->prep_cv.notify_all();
     return TCYM_OK;
 }
 
@@ -272,5 +396,21 @@ extern "C" int tcym_server_stats(tcym_server srv, tcym_server_info *out) {
     out->failed = srv->failed;
     out->bytes_in_use = srv->used;
     out->link_updates = srv->link_updates;
+    out->preparing = srv->preparing + (int)srv->ready.size();
+    out->ticks = srv->ticks;
+    out->prep_seconds = srv->prep_seconds;
+    return TCYM_OK;
+}
+
+extern "C" int tcym_server_ticks(tcym_server srv, double *ms, double *preparing, int capacity, int *n) {
+    if (!srv || capacity < 0) return TCYM_ERR_ARG;
+    std::lock_guard<std::mutex> g(srv->mu);
+    const int total = (int)srv->tick_ms.size();
+    const int k = std::min(total, capacity);
+    for (int i = 0; i < k; ++i) {
+        if (ms) ms[i] = srv->tick_ms[total - k + i];
+        if (preparing) preparing[i] = srv->tick_prep[total - k + i];
+    }
+    if (n) *n = k;
     return TCYM_OK;
 }

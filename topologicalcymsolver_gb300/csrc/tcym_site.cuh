@@ -59,27 +59,95 @@ TCYM_HD typename F::Mat staple_sum(const void *U, int64_t V, const Nbhd &nb, int
     return A;
 }
 
+// Sum of the lower staples around U_mu(x), sum_{nu != mu} cnu[nu] S-, S- as above.
+template <class F>
+TCYM_HD typename F::Mat lower_staple_sum(const void *U, int64_t V, const Nbhd &nb, int mu,
+                                         const typename F::T (&cnu)[3]) {
+    using G = typename F::G;
+    using M = typename F::Mat;
+    M A = G::zero();
+#pragma unroll
+    for (int k = 1; k <= 2; ++k) {
+        const int nu = mu + k >= 3 ? mu + k - 3 : mu + k;
+        M b1 = F::load(U, V, nu, nb.at(mu, 1, nu, -1));
+        const int64_t sb = nb.at(nu, -1);
+        M b2 = F::load(U, V, mu, sb);
+        M b3 = F::load(U, V, nu, sb);
+        M lo = G::template mulu<false, false>(G::template mulu<true, true>(b1, b2), b3);
+        A = G::add(A, G::scale(sel3(cnu, nu), lo));
+    }
+    return A;
+}
+
+// the group arithmetic of a format in the working type T: packed pairs (f2) or scalars
+template <class F, class T, bool PACKED = std::is_same<T, f2>::value> struct GroupOf { using type = typename F::G; };
+template <class F, class T> struct GroupOf<F, T, true> { using type = typename F::G2; };
+
+// The step's force with the plaquettes shared between directions.  The force on
+// U_mu(x) sums, over nu != mu, the projections of the plaquette above the link
+// (corner x) and of the one below it (corner x - nu).  The plaquette above is
+// P_{mu nu}(x) = U_mu(x) S+_{mu nu}, and P_{nu mu}(x) = P_{mu nu}(x)^dag, whose
+// projection is the negative, so the upper staples of all six (mu, nu) come from
+// the three plaquettes P_01, P_12, P_20 at x, each formed once:
+//   f_mu = c_{mu+1} p_{mu,mu+1} - c_{mu+2} p_{mu+2,mu} + proj(U_mu sum_nu c_nu S-_{mu nu})
+// with p_{mu nu} = proj(P_{mu nu}(x)).  That is the reference's bracket
+// (Dynamics.cpp:184-188) in the staple form above, with 18 instead of 24 SU(3)
+// products per site.  plaquette_projections writes p_01, p_12, p_20 to
+// sm[(k * NA + a) * stride], the caller's slots for this site (shared memory
+// on the device), where the per-direction phase reads them back.
+template <class F, class M, class T, class LOAD>
+TCYM_HD void plaquette_projections(LOAD load, T *sm, int stride) {
+    using G = typename GroupOf<F, T>::type;
+#pragma unroll 1
+    for (int mu = 0; mu < 3; ++mu) {
+        const int nu = mu == 2 ? 0 : mu + 1;
+        // P_{mu nu}(x) = [U_mu(x) U_nu(x+mu)] [U_nu(x) U_mu(x+nu)]^dag
+        const M t1 = G::template mulu<false, false>(load(mu, 0, mu), load(nu, 1, mu));
+        const M t2 = G::template mulu<false, false>(load(nu, 0, mu), load(mu, 1, nu));
+        T pr[F::NA];
+        G::proj_mul_dag(t1, t2, pr);
+#pragma unroll
+        for (int a = 0; a < F::NA; ++a) sm[(mu * F::NA + a) * stride] = pr[a];
+    }
+}
+// f[a] += c_{mu+1} p_{mu,mu+1} - c_{mu+2} p_{mu+2,mu}
+template <int NA, class T, class C>
+TCYM_HD void add_plaquette_force(const T *sm, int stride, int mu, const C (&cnu)[3], T *f) {
+    const int n1 = mu == 2 ? 0 : mu + 1, n2 = mu == 0 ? 2 : mu - 1;
+    const T cp(sel3(cnu, n1)), cm(sel3(cnu, n2));
+#pragma unroll
+    for (int a = 0; a < NA; ++a) f[a] = fma(cp, sm[(mu * NA + a) * stride], fma(-cm, sm[(n2 * NA + a) * stride], f[a]));
+}
+
 // One site of a step.  DO_E: compute the force and update E; DO_U: move the
 // links by exp(i uc E) and write them to Uout (Uout may alias Uin only when
-// DO_E is false, i.e. for the pointwise link update).
+// DO_E is false, i.e. for the pointwise link update).  sm: 3 * NA slots of T
+// for this site, stride apart (used when DO_E).
 template <class F, bool DO_E, bool DO_U>
 TCYM_HD void site_step(const Geom &g, const void *Uin, void *Uout, void *E, const StepCoef<typename F::T> &c,
-                       int64_t s, uint64_t step_add = 0) {
+                       int64_t s, uint64_t step_add, typename F::T *sm, int stride) {
     using G = typename F::G;
     using T = typename F::T;
     using M = typename F::Mat;
     constexpr int NA = F::NA;
     const int64_t V = g.V;
     Nbhd nb(g, s);
+    if (DO_E) {
+        // link along d at x (a = 0) or at x + e_dir (a = 1)
+        auto load = [&](int d, int a, int dir) { return F::load(Uin, V, d, a ? nb.at(dir, 1) : s); };
+        plaquette_projections<F, M>(load, sm, stride);
+    }
 #pragma unroll 1
     for (int mu = 0; mu < 3; ++mu) {
         T e[NA];
-        F::load_e(E, V, mu, s, e);
-        M u = F::load(Uin, V, mu, s);
+        M u;
         if (DO_E) {
-            M A = staple_sum<F>(Uin, V, nb, mu, c.cnu);
+            const M A = lower_staple_sum<F>(Uin, V, nb, mu, c.cnu);
+            u = F::load(Uin, V, mu, s);
+            F::load_e(E, V, mu, s, e);
             T f[NA];
             G::proj_mul(u, A, f);
+            add_plaquette_force<NA>(sm, stride, mu, c.cnu, f);
             const T fc = sel3(c.fc, mu);
             if (c.mode == MODE_LANGEVIN) {
                 T xi[NA];
@@ -95,6 +163,9 @@ TCYM_HD void site_step(const Geom &g, const void *Uin, void *Uout, void *E, cons
                 for (int a = 0; a < NA; ++a) e[a] = e[a] + fc * f[a];
             }
             F::store_e(E, V, mu, s, e);
+        } else {
+            u = F::load(Uin, V, mu, s);
+            F::load_e(E, V, mu, s, e);
         }
         if (DO_U) {
             F::store(Uout, V, mu, s, G::iexp_mul(sel3(c.uc, mu), e, u));
@@ -103,42 +174,6 @@ TCYM_HD void site_step(const Geom &g, const void *Uin, void *Uout, void *E, cons
 }
 
 // ------------------------------------------------------------------ site pairs
-#ifndef TCYM_PAIR_STAPLE_UNROLL
-#define TCYM_PAIR_STAPLE_UNROLL 2
-#endif
-constexpr int kPairStapleUnroll = TCYM_PAIR_STAPLE_UNROLL;
-#ifndef TCYM_PAIR_LATE_LOADS
-#define TCYM_PAIR_LATE_LOADS 1
-#endif  // 1: one copy of the staple code for both planes
-// site_step for both sites of pair p of an FP32 lattice with even nz, (x,y,z)
-// and (x,y,z+nz/2), in packed FP32 (f2): the same staples, projection, E
-// update and exponential per lane, at half the instructions.  SEAM: the pair
-// may touch the seam z = nz/2, across which neighbour pairs arrive with their
-// lanes swapped; pairs away from it skip the swap tests.
-template <class F, bool SEAM>
-TCYM_HD typename F::Mat2 staple_sum_pair(const void *U, int64_t Vh, const PairNbhd &nb, int mu,
-                                         const float (&cnu)[3]) {
-    using G2 = typename F::G2;
-    using M2 = typename F::Mat2;
-    M2 A = G2::zero();
-#pragma unroll kPairStapleUnroll
-    for (int k = 1; k <= 2; ++k) {
-        const int nu = mu + k >= 3 ? mu + k - 3 : mu + k;
-        M2 a1 = F::load2(U, Vh, nu, nb.at(mu, 1), SEAM && nb.swapped(mu, 1));
-        M2 a2 = F::load2(U, Vh, mu, nb.at(nu, 1), SEAM && nb.swapped(nu, 1));
-        M2 a3 = F::load2(U, Vh, nu, nb.p, false);
-        M2 up = G2::template mulu<false, true>(G2::template mulu<false, true>(a1, a2), a3);
-        M2 b1 = F::load2(U, Vh, nu, nb.at(mu, 1, nu, -1), SEAM && nb.swapped(mu, 1, nu, -1));
-        const int64_t sb = nb.at(nu, -1);
-        const bool wb = SEAM && nb.swapped(nu, -1);
-        M2 b2 = F::load2(U, Vh, mu, sb, wb);
-        M2 b3 = F::load2(U, Vh, nu, sb, wb);
-        M2 lo = G2::template mulu<false, false>(G2::template mulu<true, true>(b1, b2), b3);
-        A = G2::add(A, G2::scale(f2(sel3(cnu, nu)), G2::add(up, lo)));
-    }
-    return A;
-}
-
 // E += fc f - damp E + kick xi for both sites of pair p (Philox noise of sites p, p + Vh)
 template <int NA>
 TCYM_COLD void langevin_kick_pair(const StepCoef<float> &c, int mu, int64_t p, int64_t Vh, uint64_t step_add, f2 fc,
@@ -151,35 +186,54 @@ TCYM_COLD void langevin_kick_pair(const StepCoef<float> &c, int mu, int64_t p, i
     for (int a = 0; a < NA; ++a) e[a] = e[a] + fma(kick, f2(x0[a], x1[a]), fma(-damp, e[a], fc * f[a]));
 }
 
+// site_step for both sites of pair p of an FP32 lattice with even nz, (x,y,z)
+// and (x,y,z+nz/2), in packed FP32 (f2): the same plaquettes, staples,
+// projections, E update and exponential per lane, at half the instructions.
+// SEAM: the pair may touch the seam z = nz/2, across which neighbour pairs
+// arrive with their lanes swapped; pairs away from it skip the swap tests.
 // cn: the Langevin noise's coefficients (seed, step, damping, kick), which may
 // sit apart from the step's (a batched member's own, beside coefficients the
 // members share).  MODE >= 0 fixes the step kind at compile time (c.mode is
-// then ignored); -1 reads it from c.
+// then ignored); -1 reads it from c.  sm: 3 * NA f2 slots for this pair,
+// stride apart (shared memory on the device).
+// The plaquette form (see plaquette_projections) took the SU(3) step from
+// 0.366 to 0.331 ms per 128^3 step on GB300 and, needing fewer registers,
+// runs 4 blocks of 128 per SM without spills (the staple form: 3).
 template <class F, bool SEAM, int MODE = -1>
 TCYM_HD void site_step_pair(const Geom &g, const void *Uin, void *Uout, void *E, const StepCoef<float> &c,
-                            const StepCoef<float> &cn, int64_t p, uint64_t step_add) {
+                            const StepCoef<float> &cn, int64_t p, uint64_t step_add, f2 *sm, int stride) {
     using G2 = typename F::G2;
     using M2 = typename F::Mat2;
     constexpr int NA = F::NA;
     const int64_t Vh = g.V >> 1;
     const PairNbhd nb(g, p);
+    auto load = [&](int d, int a, int dir) {
+        return a ? F::load2(Uin, Vh, d, nb.at(dir, 1), SEAM && nb.swapped(dir, 1)) : F::load2(Uin, Vh, d, p, false);
+    };
+    plaquette_projections<F, M2>(load, sm, stride);
 #pragma unroll 1
     for (int mu = 0; mu < 3; ++mu) {
-#if TCYM_PAIR_LATE_LOADS
+        // lower staples S- = U_nu^dag(x+mu-nu) U_mu^dag(x-nu) U_nu(x-nu)
+        M2 A = G2::zero();
+#pragma unroll
+        for (int k = 1; k <= 2; ++k) {
+            const int nu = mu + k >= 3 ? mu + k - 3 : mu + k;
+            const M2 b1 = F::load2(Uin, Vh, nu, nb.at(mu, 1, nu, -1), SEAM && nb.swapped(mu, 1, nu, -1));
+            const int64_t sb = nb.at(nu, -1);
+            const bool wb = SEAM && nb.swapped(nu, -1);
+            const M2 b2 = F::load2(Uin, Vh, mu, sb, wb);
+            const M2 b3 = F::load2(Uin, Vh, nu, sb, wb);
+            const M2 lo = G2::template mulu<false, false>(G2::template mulu<true, true>(b1, b2), b3);
+            A = G2::add(A, G2::scale(f2(sel3(c.cnu, nu)), lo));
+        }
         // the link and its field are read after the staple sum, so that they are
-        // not live (36 + 16 registers) while it runs
-        const M2 A = staple_sum_pair<F, SEAM>(Uin, Vh, nb, mu, c.cnu);
+        // not live while it runs
         const M2 u = F::load2(Uin, Vh, mu, p, false);
         f2 e[NA];
         F::load_e2(E, Vh, mu, p, e);
-#else
-        f2 e[NA];
-        F::load_e2(E, Vh, mu, p, e);
-        const M2 u = F::load2(Uin, Vh, mu, p, false);
-        const M2 A = staple_sum_pair<F, SEAM>(Uin, Vh, nb, mu, c.cnu);
-#endif
         f2 f[NA];
         G2::proj_mul(u, A, f);
+        add_plaquette_force<NA>(sm, stride, mu, c.cnu, f);
         const f2 fc(sel3(c.fc, mu));
         const int mode = MODE >= 0 ? MODE : c.mode;
         if (mode == MODE_LANGEVIN) {
@@ -198,80 +252,8 @@ TCYM_HD void site_step_pair(const Geom &g, const void *Uin, void *Uout, void *E,
 
 template <class F, bool SEAM, int MODE = -1>
 TCYM_HD void site_step_pair(const Geom &g, const void *Uin, void *Uout, void *E, const StepCoef<float> &c, int64_t p,
-                            uint64_t step_add = 0) {
-    site_step_pair<F, SEAM, MODE>(g, Uin, Uout, E, c, c, p, step_add);
-}
-
-// site_step_pair with the plaquettes shared between directions.  The force on
-// U_mu(x) sums, over nu != mu, the projections of the plaquette above the link
-// (corner x) and of the one below it (corner x - nu); the plaquette above is
-// P_{mu nu}(x) = U_mu(x) S+, and P_{nu mu}(x) = P_{mu nu}(x)^dag, whose
-// projection is the negative.  So the upper staples of all six (mu, nu) come
-// from the three plaquettes P_01, P_12, P_20 at x, each formed once:
-//   f_mu = c_{mu+1} p_{mu,mu+1} - c_{mu+2} p_{mu+2,mu} + proj(U_mu sum_nu c_nu S-_{mu nu})
-// which is the bracket of Dynamics.cpp:184-188 in the staple form above, with 18
-// instead of 24 SU(3) products per site.  The three projections wait in `sm`
-// (this thread's slots, stride `stride`: [plaquette][component]) between the
-// plaquette phase and the per-direction phase.
-template <class F, bool SEAM, int MODE = -1>
-TCYM_HD void site_step_pair_plaq(const Geom &g, const void *Uin, void *Uout, void *E, const StepCoef<float> &c,
-                                 const StepCoef<float> &cn, int64_t p, uint64_t step_add, f2 *sm, int stride) {
-    using G2 = typename F::G2;
-    using M2 = typename F::Mat2;
-    constexpr int NA = F::NA;
-    const int64_t Vh = g.V >> 1;
-    const PairNbhd nb(g, p);
-    // P_{mu nu}(x) = [U_mu(x) U_nu(x+mu)] [U_nu(x) U_mu(x+nu)]^dag, (mu, nu) = (0,1), (1,2), (2,0)
-#pragma unroll 1
-    for (int mu = 0; mu < 3; ++mu) {
-        const int nu = mu == 2 ? 0 : mu + 1;
-        const M2 t1 = G2::template mulu<false, false>(F::load2(Uin, Vh, mu, p, false),
-                                                      F::load2(Uin, Vh, nu, nb.at(mu, 1), SEAM && nb.swapped(mu, 1)));
-        const M2 t2 = G2::template mulu<false, false>(F::load2(Uin, Vh, nu, p, false),
-                                                      F::load2(Uin, Vh, mu, nb.at(nu, 1), SEAM && nb.swapped(nu, 1)));
-        f2 pr[NA];
-        G2::proj_mul_dag(t1, t2, pr);
-#pragma unroll
-        for (int a = 0; a < NA; ++a) sm[(mu * NA + a) * stride] = pr[a];
-    }
-#pragma unroll 1
-    for (int mu = 0; mu < 3; ++mu) {
-        // lower staples S- = U_nu^dag(x+mu-nu) U_mu^dag(x-nu) U_nu(x-nu)
-        M2 A = G2::zero();
-#pragma unroll
-        for (int k = 1; k <= 2; ++k) {
-            const int nu = mu + k >= 3 ? mu + k - 3 : mu + k;
-            const M2 b1 = F::load2(Uin, Vh, nu, nb.at(mu, 1, nu, -1), SEAM && nb.swapped(mu, 1, nu, -1));
-            const int64_t sb = nb.at(nu, -1);
-            const bool wb = SEAM && nb.swapped(nu, -1);
-            const M2 b2 = F::load2(Uin, Vh, mu, sb, wb);
-            const M2 b3 = F::load2(Uin, Vh, nu, sb, wb);
-            const M2 lo = G2::template mulu<false, false>(G2::template mulu<true, true>(b1, b2), b3);
-            A = G2::add(A, G2::scale(f2(sel3(c.cnu, nu)), lo));
-        }
-        const M2 u = F::load2(Uin, Vh, mu, p, false);
-        f2 e[NA];
-        F::load_e2(E, Vh, mu, p, e);
-        f2 f[NA];
-        G2::proj_mul(u, A, f);
-        const int n1 = mu == 2 ? 0 : mu + 1, n2 = mu == 0 ? 2 : mu - 1;
-        const f2 cp(sel3(c.cnu, n1)), cm(sel3(c.cnu, n2));
-#pragma unroll
-        for (int a = 0; a < NA; ++a) f[a] = fma(cp, sm[(mu * NA + a) * stride], fma(-cm, sm[(n2 * NA + a) * stride], f[a]));
-        const f2 fc(sel3(c.fc, mu));
-        const int mode = MODE >= 0 ? MODE : c.mode;
-        if (mode == MODE_LANGEVIN) {
-            langevin_kick_pair<NA>(cn, mu, p, Vh, step_add, fc, f, e);
-        } else if (mode == MODE_FLOW) {
-#pragma unroll
-            for (int a = 0; a < NA; ++a) e[a] = fc * f[a];
-        } else {
-#pragma unroll
-            for (int a = 0; a < NA; ++a) e[a] = fma(fc, f[a], e[a]);
-        }
-        F::store_e2(E, Vh, mu, p, e);
-        F::store2(Uout, Vh, mu, p, G2::iexp_mul(f2(sel3(c.uc, mu)), e, u));
-    }
+                            uint64_t step_add, f2 *sm, int stride) {
+    site_step_pair<F, SEAM, MODE>(g, Uin, Uout, E, c, c, p, step_add, sm, stride);
 }
 
 // Does the block of pairs [p0, p0 + n) touch the seam planes z = 0 or z = nz/2 - 1?

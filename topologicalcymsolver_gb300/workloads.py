@@ -6,7 +6,8 @@ ensemble: 256 independent thermal leapfrog trajectories, each SU(2) or SU(3)
   in FP64 to 1e-10, stepped in FP32 storage with FP64 reductions, in batched
   graph-captured launches (tcym_ensemble_*).  Compared with the same lattices
   stepped by per-lattice launches and with the plain FP64 path.
-serve: a Poisson request stream at 80% of the measured sustainable throughput;
+serve: a Poisson request stream at 80% of the measured sustainable throughput (the
+  steady-state rate of a server kept full by a closed loop of 48 requests in flight);
   each request: SU(2)/SU(3) 50/50, L uniform over {24, 32, 48, 64, 96, 128}
   (log-spaced, so uniform in log L), T uniform in [0.3, 1.0], leapfrog or
   Langevin (gamma = 1) 50/50, steps log-uniform in [1000, 20000], N_CS(t)
@@ -136,6 +137,38 @@ def _work(r, stride=20):
     return 3 * r["L"] ** 3 * int(math.ceil(r["nsteps"] / stride) * stride)
 
 
+def sustainable_rate(ctx, budget, dt, in_flight=48, warm_s=5.0, window_s=30.0, seed=60):
+    """Aggregate link-updates/s of a server kept full: a closed loop holds `in_flight`
+    requests from the request distribution queued or running, replacing each one as it
+    finishes, and the server's link-update counter is read over `window_s` seconds after
+    `warm_s` of ramp-up.  The server is closed afterwards (its requests abandoned)."""
+    srv = Server(ctx, budget, max_active=512, stride=20)
+    pool = serve_requests(100000, seed=seed)
+    k, live = 0, []
+
+    def top_up():
+        nonlocal k
+        while len(live) < in_flight:
+            r = pool[k]
+            k += 1
+            live.append(srv.submit(nc=r["nc"], L=r["L"], T=r["T"], nsteps=r["nsteps"], dynamics=r["dynamics"],
+                                   dt=dt[r["dynamics"]], gamma=1.0, precision=FP32, seed=r["seed"]))
+
+    top_up()
+    t0, mark = time.perf_counter(), None
+    while True:
+        live[:] = [i for i in live if srv.status(i)[0] in (0, 1)]
+        top_up()
+        now = time.perf_counter()
+        if mark is None and now - t0 >= warm_s:
+            mark = (now, srv.stats()["link_updates"])
+        elif mark is not None and now - mark[0] >= window_s:
+            rate = (srv.stats()["link_updates"] - mark[1]) / (now - mark[0])
+            srv.close()
+            return rate
+        time.sleep(0.02)
+
+
 def run_serve(a):
     ctx = Context(0)
     reqs = serve_requests(a.requests)
@@ -147,13 +180,8 @@ def run_serve(a):
         return srv.submit(nc=r["nc"], L=r["L"], T=r["T"], nsteps=r["nsteps"], dynamics=r["dynamics"],
                           dt=dt[r["dynamics"]], gamma=1.0, precision=FP32, seed=r["seed"])
 
-    # sustainable throughput: a saturating batch drawn from the same distribution
-    sat = serve_requests(min(32, a.requests), seed=60)
-    t0 = time.perf_counter()
-    ids = [submit(r) for r in sat]
-    for i in ids:
-        srv.wait(i, 3600)
-    sustainable = sum(_work(r) for r in sat) / (time.perf_counter() - t0)
+    # sustainable throughput: the steady state of a server kept full (on its own server)
+    sustainable = sustainable_rate(ctx, budget, dt, window_s=getattr(a, "serve_window", 30.0))
     # Poisson arrivals at 80% of it
     mean_work = sum(_work(r) for r in reqs) / len(reqs)
     lam = 0.8 * sustainable / mean_work
@@ -175,6 +203,7 @@ def run_serve(a):
         lat_s.append(latency)
     makespan = time.perf_counter() - start
     stats = srv.stats()
+    tick_ms, tick_prep = srv.ticks()
     srv.close()
     ctx.close()
     total = sum(_work(r) for r in reqs)
@@ -188,6 +217,13 @@ def run_serve(a):
         "p50_latency_s": float(np.percentile(lat_s, 50)), "p99_latency_s": float(np.percentile(lat_s, 99)),
         "requests": len(reqs), "failed": failed, "sustainable_link_updates_per_s": sustainable,
         "offered_requests_per_s": lam, "makespan_s": makespan, "server_link_updates": stats["link_updates"],
+        "prep_seconds": stats["prep_seconds"], "ticks": stats["ticks"],
+        "tick_ms": {"median": float(np.median(tick_ms)) if len(tick_ms) else None,
+                    "median_while_preparing": (float(np.median(tick_ms[tick_prep > 0]))
+                                               if np.any(tick_prep > 0) else None),
+                    "median_idle_preparers": (float(np.median(tick_ms[tick_prep == 0]))
+                                              if np.any(tick_prep == 0) else None),
+                    "note": "last <= 8192 ticks; a tick = stride steps of every running request + its N_CS sample"},
     }
 
 
