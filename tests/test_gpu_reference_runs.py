@@ -8,11 +8,11 @@ SU(3) 64^3 Langevin: dt 0.02, gamma 1, T 0.6, links exp(i theta lambda/2)
   theta ~ N(0, 0.09) (seed 2), E = 0, noise seed 3: pointwise against the FP64
   oracle fed the identical noise for 100 steps (FP64 <= 1e-10, FP32 <= 1e-5
   relative), and the Kahan-integrated N_CS over the first 10.
-SU(2) 96^3 cooling: leapfrog, then checkerboarded gradient-flow cooling sweeps at
-  dtau 0.02: at 32^3 against the oracle's checkerboard restatement every 10
-  sweeps; at the full 96^3 (2000 leapfrog steps, 500 sweeps) FP32 storage
-  against the FP64 path over the first 30 sweeps, and the energy decaying
-  monotonically over all 500 in both.
+SU(2) 96^3 cooling: leapfrog, then gradient-flow cooling sweeps at dtau 0.02:
+  at 32^3 against the oracle's checkerboard restatement every 10 sweeps; at the
+  full 96^3 (2000 leapfrog steps, 500 sweeps) the FP32 checkerboard series
+  against the oracle's and the FP64 simultaneous series against the reference's
+  own (tests/golden/ref_cooling_su2_96.npz).
 energy: over 10^4 leapfrog steps neither path's mean energy drifts and the
   FP32 path's stays with the FP64 path's.
 """
@@ -138,23 +138,52 @@ def test_su2_cooling_sweeps_against_oracle(ctx, oracle_port, prec, tol, tol_mag)
     assert all(b < a for a, b in zip(mags, mags[1:]))  # cooling lowers the magnetic energy
 
 
-def test_su2_96_cooling_fp32_tracks_fp64(ctx):
+def test_su2_96_cooling_against_reference_run(ctx):
+    """The SU(2) 96^3 cooling run at full size against tests/golden/ref_cooling_su2_96.npz:
+    U = 1, E ~ N(0, 1/2) (seed 4) restored as the reference restores (1e-14, at most
+    10000 iterations), 2000 leapfrog steps in FP64 (the start matches the reference's
+    own, sampled at 64 sites and through its observables), then 500 sweeps of dtau 0.02
+    with energy and cooled N_CS (improved E.B, trapezoid along the flow) every 10 sweeps:
+    FP32-storage checkerboard sweeps against the oracle's checkerboard series, and FP64
+    simultaneous sweeps against the reference's own CalibrationUpdate series."""
+    d = dict(np.load(os.path.join(G, "ref_cooling_su2_96.npz")))
     shape = (96, 96, 96)
-    l64 = _cooling_input(ctx, shape, 2000, tol=1e-12)
+    l64 = tcym.Lattice(ctx, 2, shape, tcym.FP64)
+    l64.set_zero()
+    l64.gaussian_efield(np.sqrt(0.5), 4)
+    l64.gauss_restore(1e-14, 10000)
+    l64.leapfrog(0.05, 2000)
+    U, E = l64.download()
+    idx = d["fp_sites"]
+    fp_u, fp_e = rel(U[idx], d["fp_U"]), rel(E[idx], d["fp_E"])
+    o = l64.observables().as_oracle_vector()
+    fp_t = abs(o[0] / d["start_obs"][0] - 1)
     l32 = tcym.Lattice(ctx, 2, shape, tcym.FP32)
     l32.copy_from(l64)
-    m64, m32 = [], []
-    for _ in range(50):  # 500 sweeps, energies every 10
-        for lat, m in ((l64, m64), (l32, m32)):
-            lat.flow(0.02, 10, tcym.FLOW_CHECKERBOARD)
-            m.append(lat.observables().magnetic)
-    m64, m32 = np.array(m64), np.array(m32)
-    # both cool monotonically to below 1% of the first record
-    assert np.all(np.diff(m64) < 0) and np.all(np.diff(m32) < 0)
-    assert m64[-1] < 0.01 * m64[0] and m32[-1] < 0.01 * m32[0]
-    # pointwise over the first 30 sweeps; later the flow nears saddle points whose unstable
-    # directions amplify any difference (FP32 against FP64 grows ~3x per 10 sweeps there)
-    assert np.abs(m32[:3] / m64[:3] - 1).max() < 1e-5, np.abs(m32 / m64 - 1)[:6]
+    cb, sim = d["checkerboard"], d["simultaneous"]
+    got32, got64, t32, t64 = [], [], 0.0, 0.0
+    for _ in range(len(cb)):
+        t32 += l32.flow(0.02, 10, tcym.FLOW_CHECKERBOARD, calibrate=tcym.NCS_IMPROVED)
+        t64 += l64.flow(0.02, 10, tcym.FLOW_SIMULTANEOUS, calibrate=tcym.NCS_IMPROVED)
+        a, b = l32.observables(), l64.observables()
+        got32.append([a.T00, a.electric, a.magnetic, t32])
+        got64.append([b.T00, b.electric, b.magnetic, t64])
+    got32, got64 = np.array(got32), np.array(got64)
+    mag32 = np.abs(got32[:, 2] / cb[:, 2] - 1)
+    mag64 = np.abs(got64[:, 2] / sim[:, 2] - 1)
+    dscale = np.abs(np.diff(np.concatenate([[0.0], cb[:, 3]]))).max()  # the largest 10-sweep increment
+    ncs32 = np.abs(got32[:, 3] - cb[:, 3]) / dscale
+    ncs64 = np.abs(got64[:, 3] - sim[:, 3]) / np.abs(np.diff(np.concatenate([[0.0], sim[:, 3]]))).max()
+    print(f"\nmeasured SU(2) 96^3 cooling: start U {fp_u:.2e} E {fp_e:.2e} T00 {fp_t:.2e}; FP32 checkerboard "
+          f"magnetic {mag32[:3].max():.2e} (30 sweeps) {mag32.max():.2e} (500), N_CS {ncs32[:3].max():.2e} / "
+          f"{ncs32.max():.2e}; FP64 simultaneous magnetic {mag64[:3].max():.2e} / {mag64.max():.2e}, N_CS "
+          f"{ncs64[:3].max():.2e} / {ncs64.max():.2e}")
+    assert fp_u < 1e-9 and fp_e < 1e-9 and fp_t < 1e-10
+    assert np.all(np.diff(got32[:, 2]) < 0) and np.all(np.diff(got64[:, 2]) < 0)  # cooling lowers B^2
+    assert mag32[:3].max() < 1e-5 and ncs32[:3].max() < 1e-5
+    assert mag64[:3].max() < 1e-9 and ncs64[:3].max() < 1e-9
+    assert mag32.max() < 1e-3 and ncs32.max() < 1e-3
+    assert mag64.max() < 1e-6 and ncs64.max() < 1e-6
 
 
 def test_energy_drift_fp32_vs_fp64(ctx):
