@@ -270,6 +270,8 @@ template <class T> struct SU3 {
     using real = T;
     using Mat = M3<T>;
     static constexpr int NA = 8;
+    // FP32 arithmetic, one value or a packed pair (the series lengths depend on it)
+    static constexpr bool kSingle = sizeof(T) == 4 || Packed<T>::value;
 
     static TCYM_HD Mat identity() {
         Mat r;
@@ -468,7 +470,7 @@ template <class T> struct SU3 {
                   q.m[0][2] * (q.m[1][0] * q.m[2][1] - q.m[1][1] * q.m[2][0]);
         T c0 = d.re;
         // sum_n (i^n / n!) Q^n with Q^n = a_n + b_n Q + d_n Q^2
-        const int N = sizeof(T) == 4 ? 9 : 16;
+        const int N = kSingle ? 9 : 16;
         T a = T(1), b = T(0), dd = T(0);
         T f0r = T(1), f0i = T(0), f1r = T(0), f1i = T(0), f2r = T(0), f2i = T(0);
         T fact = T(1);
@@ -534,7 +536,15 @@ template <class T> struct SU3 {
                      T(2) * (q.m[0][1].re * (q.m[1][2].re * q.m[2][0].re - q.m[1][2].im * q.m[2][0].im) -
                              q.m[0][1].im * (q.m[1][2].re * q.m[2][0].im + q.m[1][2].im * q.m[2][0].re));
         T f0r, f0i, f1r, f1i, f2r, f2i;
-        series_coeffs(c0, c1, f0r, f0i, f1r, f1i, f2r, f2i);
+        if constexpr (kSingle) {
+            // terms of the series by the spectral radius r (r^2 <= 4 c1 / 3): the first
+            // omitted term r^(N+1)/(N+1)! stays below half an FP32 ulp, 3e-8, with 5
+            // terms for r^2 <= 0.02 (the common case: |dt E| is small) and 8 up to r = 1/2
+            if (any_gt(c1 * T(4.0 / 3.0), T(0.02))) series_coeffs<8>(c0, c1, f0r, f0i, f1r, f1i, f2r, f2i);
+            else series_coeffs<5>(c0, c1, f0r, f0i, f1r, f1i, f2r, f2i);
+        } else {
+            series_coeffs<16>(c0, c1, f0r, f0i, f1r, f1i, f2r, f2i);
+        }
         Mat w;
 #pragma unroll
         for (int i = 0; i < 2; ++i)
@@ -575,8 +585,8 @@ template <class T> struct SU3 {
 
     // f_k of exp(iQ) = f0 + f1 Q + f2 Q^2 for spectral radius <= 1/2: the Taylor
     // series reduced with Q^3 = c1 Q + c0 (Q^n = a_n + b_n Q + d_n Q^2).
-    static TCYM_HD void series_coeffs(T c0, T c1, T &f0r, T &f0i, T &f1r, T &f1i, T &f2r, T &f2i) {
-        constexpr int N = sizeof(T) == 4 ? 9 : 16;
+    template <int N> static TCYM_HD void series_coeffs(T c0, T c1, T &f0r, T &f0i, T &f1r, T &f1i, T &f2r, T &f2i) {
+        static_assert(N >= 1 && N <= 16, "at most 16 terms");
         constexpr double inv_fact[17] = {1.0, 1.0, 0.5, 1.0 / 6, 1.0 / 24, 1.0 / 120, 1.0 / 720, 1.0 / 5040,
                                          1.0 / 40320, 1.0 / 362880, 1.0 / 3628800, 1.0 / 39916800,
                                          1.0 / 479001600, 1.0 / 6227020800.0, 1.0 / 87178291200.0,
