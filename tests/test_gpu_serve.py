@@ -103,11 +103,11 @@ def test_bounded_wait_and_injected_fault(ctx):
 
 
 def test_ticks_continue_while_a_large_request_is_prepared(ctx):
-    """Eight small requests tick; a 128^3 SU(3) request arrives, whose preparation
-    (FP64 lattice, Gaussian fields, Gauss restore to 1e-12, conversion to FP32) takes
-    far longer than a tick.  The ticks during that preparation stay close to the ticks
-    before it (measured: 0.29 ms before, 0.94 ms median during a 7 s preparation): the
-    loop does not stop for an admission."""
+    """Eight small requests tick; a 128^3 SU(3) FP64 request arrives, whose preparation
+    (Gaussian fields, Gauss restore to 1e-12 in FP64) takes far longer than a tick.  The
+    ticks during that preparation stay close to the ticks before it (measured: 0.3 ms
+    before, 0.84-0.95 ms median during a 7 s preparation): the loop does not stop for
+    an admission."""
     s = tcym.Server(ctx, 64 * GB, stride=20)
     small = [s.submit(nc=2, L=24, T=0.5, nsteps=400000, seed=i) for i in range(8)]
     t0 = time.time()
@@ -116,7 +116,7 @@ def test_ticks_continue_while_a_large_request_is_prepared(ctx):
     time.sleep(0.5)
     ms, _ = s.ticks()
     base = float(np.median(ms[-100:]))
-    big = s.submit(nc=3, L=128, T=0.6, nsteps=20, precision=tcym.FP32, seed=99)
+    big = s.submit(nc=3, L=128, T=0.6, nsteps=20, precision=tcym.FP64, seed=99)
     assert s.wait(big, 300) == 0
     ms, prep = s.ticks()
     during = ms[prep > 0]

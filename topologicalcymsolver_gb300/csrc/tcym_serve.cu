@@ -7,9 +7,8 @@
 //   * preparer threads take requests in arrival order while the device-memory
 //     budget and the slot limit allow, and build each one's initial state on the
 //     request's own stream: U = 1, E ~ N(0, T) from the request's Philox field
-//     stream, Gauss-restored in FP64 (a temporary FP64 lattice for FP32 requests,
-//     copied into FP32 storage) -- the restore queues its iterations in batches
-//     and learns of convergence from a device-side flag;
+//     stream, Gauss-restored in the request's own storage -- the restore queues
+//     its iterations in batches and learns of convergence from a device-side flag;
 //   * the tick thread owns the running ensemble: at each tick boundary it joins
 //     the prepared requests, advances every running request `stride` steps in
 //     the ensemble's batched launches, appends (steps, N_CS) per request and
@@ -67,14 +66,9 @@ size_t lattice_bytes(int fmt, size_t V, int sm_count) {
 void footprint_of(const tcym_request &r, int sm_count, size_t &running, size_t &extra) {
     const int fmt = tcym_format_of(r.nc, r.precision);
     const size_t V = (size_t)r.L * r.L * r.L;
-    const size_t na = r.nc == 2 ? 3 : 8, nmd = r.nc == 2 ? 4 : 18;
+    const size_t na = r.nc == 2 ? 3 : 8;
     running = lattice_bytes(fmt, V, sm_count);
-    // the FP64 preparation lattice with its restore scratch; FP32 requests also
-    // stage the FP64 state (AoS) for the conversion into FP32 storage
-    const int fmt64 = tcym_format_of(r.nc, TCYM_FP64);
-    extra = sizeof(double) * (na * V + 4);
-    if (r.precision != TCYM_FP64)
-        extra += lattice_bytes(fmt64, V, sm_count) + sizeof(double) * 3 * (nmd + na) * V;
+    extra = sizeof(double) * (na * V + 4);  // the restore's violation array, released once prepared
 }
 
 }  // namespace
@@ -108,23 +102,17 @@ struct tcym_server_s {
 namespace {
 
 // Initial state of a request: U = 1, E ~ N(0, T) per component (Philox field
-// stream of the request's seed), Gauss-restored in FP64 to 1e-12 (at most 400
-// iterations), in the request's storage; temporary memory is released.
+// stream of the request's seed), Gauss-restored in the request's own storage,
+// at most 400 iterations, to 1e-12 in FP64 and to 1e-6 in FP32 (the rounding of
+// FP32 fields); the restore scratch is released.  FP32 requests are not restored
+// through FP64: at config 4's mix the FP64 restore (DFMA-bound, ~4.4 s of GPU
+// time for a 128^3 SU(3) lattice) took more of the device than the stepping.
 int prepare(tcym_server srv, Req &r) {
     const tcym_request &q = r.spec;
-    tcym_lattice ic = nullptr;
-    int rc = tcym_lattice_create_pooled(srv->ctx, q.nc, q.L, q.L, q.L, TCYM_FP64, srv->pool, &ic);
-    if (!rc) rc = tcym_set_zero(ic);
-    if (!rc) rc = tcym_gaussian_efield(ic, std::sqrt(q.T), q.seed);
-    if (!rc) rc = tcym_gauss_restore(ic, 1e-12, 400, nullptr, nullptr);
-    if (!rc && q.precision == TCYM_FP64) {
-        tcym_lattice_release_scratch(ic);
-        r.lat = ic;
-        return TCYM_OK;
-    }
-    if (!rc) rc = tcym_lattice_create_pooled(srv->ctx, q.nc, q.L, q.L, q.L, q.precision, srv->pool, &r.lat);
-    if (!rc) rc = tcym_lattice_copy(r.lat, ic);
-    if (ic) tcym_lattice_destroy(ic);
+    int rc = tcym_lattice_create_pooled(srv->ctx, q.nc, q.L, q.L, q.L, q.precision, srv->pool, &r.lat);
+    if (!rc) rc = tcym_set_zero(r.lat);
+    if (!rc) rc = tcym_gaussian_efield(r.lat, std::sqrt(q.T), q.seed);
+    if (!rc) rc = tcym_gauss_restore(r.lat, q.precision == TCYM_FP64 ? 1e-12 : 1e-6, 400, nullptr, nullptr);
     if (!rc) tcym_lattice_release_scratch(r.lat);
     return rc;
 }

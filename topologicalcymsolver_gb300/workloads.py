@@ -17,7 +17,9 @@ Inputs are synthetic: seeded Philox fields with the configurations' distribution
 """
 from __future__ import annotations
 
+import json
 import math
+import sys
 import time
 
 import numpy as np
@@ -169,7 +171,7 @@ def sustainable_rate(ctx, budget, dt, in_flight=48, warm_s=5.0, window_s=30.0, s
         time.sleep(0.02)
 
 
-def run_serve(a):
+def run_serve(a, progress=sys.stderr):
     ctx = Context(0)
     reqs = serve_requests(a.requests)
     dt = {DYN_LEAPFROG: 0.05, DYN_LANGEVIN: 0.02}
@@ -181,7 +183,8 @@ def run_serve(a):
                           dt=dt[r["dynamics"]], gamma=1.0, precision=FP32, seed=r["seed"])
 
     # sustainable throughput: the steady state of a server kept full (on its own server)
-    sustainable = sustainable_rate(ctx, budget, dt, window_s=getattr(a, "serve_window", 30.0))
+    sustainable = sustainable_rate(ctx, budget, dt, warm_s=20.0, window_s=getattr(a, "serve_window", 30.0))
+    print(json.dumps({"sustainable_link_updates_per_s": sustainable}), file=progress, flush=True)
     # Poisson arrivals at 80% of it
     mean_work = sum(_work(r) for r in reqs) / len(reqs)
     lam = 0.8 * sustainable / mean_work
@@ -195,12 +198,19 @@ def run_serve(a):
             time.sleep(delay)
         ids.append(submit(r))
     lat_s, failed = [], 0
-    for i in ids:
+    for k, i in enumerate(ids):
         rc = srv.wait(i, 7200)
         series, latency, rc2 = srv.result(i)
         if rc != 0:
             failed += 1
         lat_s.append(latency)
+        if progress is not None and (k + 1) % 100 == 0:  # progress on stderr, so a cut-off run leaves data
+            st = srv.stats()
+            print(json.dumps({"progress": k + 1, "elapsed_s": time.perf_counter() - start,
+                              "p50_so_far_s": float(np.percentile(lat_s, 50)),
+                              "p99_so_far_s": float(np.percentile(lat_s, 99)), "queued": st["queued"],
+                              "active": st["active"], "link_updates": st["link_updates"],
+                              "prep_seconds": st["prep_seconds"]}), file=progress, flush=True)
     makespan = time.perf_counter() - start
     stats = srv.stats()
     tick_ms, tick_prep = srv.ticks()
