@@ -230,6 +230,29 @@ def ref_available(nc: int) -> bool:
     return os.path.exists(os.path.join(HERE, "_ref", f"libref_su{nc}.so"))
 
 
+def scipy_lapack():
+    """(path, version) of the OpenBLAS build SciPy ships, whose LAPACK exports ZGEEV as
+    ``scipy_zgeev_``, or None.  Setting TCYM_REF_LAPACK to the path makes the reference's
+    SU(3) MatrixILog call that ZGEEV instead of the restatement in ``ref_wrap.cpp``."""
+    try:
+        import glob
+
+        import scipy
+    except ImportError:
+        return None
+    libs = os.path.join(os.path.dirname(os.path.dirname(scipy.__file__)), "scipy.libs")
+    for path in sorted(glob.glob(os.path.join(libs, "libscipy_openblas*.so"))):
+        try:
+            lib = ctypes.CDLL(path)
+            lib.scipy_zgeev_
+            get = lib.scipy_openblas_get_config
+            get.restype = ctypes.c_char_p
+            return path, get().decode().split(" DYNAMIC_ARCH")[0] + f" (SciPy {scipy.__version__})"
+        except (OSError, AttributeError):
+            continue
+    return None
+
+
 class Ref:
     """The reference's own sources, compiled in place (only where the reference tree exists).
 
@@ -326,6 +349,12 @@ class Ref:
         U, _ = empty_fields(self.nc, tuple(k >> blocking for k in self.shape))
         self.lib.ref_cooling_links(_p(U))
         return U
+
+    def lapack_in_use(self) -> bool:
+        """True when the reference's ZGEEV calls go to the library TCYM_REF_LAPACK names."""
+        f = self.lib.ref_lapack_in_use
+        f.restype = ctypes.c_int
+        return bool(f())
 
     def matrix_ilog(self, c, v):
         out = np.zeros(NA[self.nc])

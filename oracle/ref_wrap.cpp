@@ -16,9 +16,13 @@
  *     kernels draw (MISC/RNG/GSLRandomNumberGenerator.cpp is not included).
  *   - LAPACK zgeev (not vendored; reached only from MatrixILog,
  *     SUNc/SU3/AlgebraOperations.cpp:186-233, through
- *     SUNc/SU3/util/ComplexEigensystem.cpp:27-55): restated below for what
- *     that call site asks of it, the eigenvalues and right eigenvectors of a
- *     3x3 complex matrix that is unitary there (a normal matrix): a cyclic
+ *     SUNc/SU3/util/ComplexEigensystem.cpp:27-55).  When the environment
+ *     variable TCYM_REF_LAPACK names a shared library that exports LAPACK's
+ *     ZGEEV (as `zgeev_`, or `scipy_zgeev_` in the OpenBLAS build that SciPy
+ *     ships), the call is forwarded to it unchanged: the reference then runs
+ *     on a real LAPACK.  Otherwise it is restated below for what that call
+ *     site asks of it, the eigenvalues and right eigenvectors of a 3x3
+ *     complex matrix that is unitary there (a normal matrix): a cyclic
  *     complex Jacobi on the Hermitian (A + A^dag)/2 + g (A - A^dag)/2i, which
  *     shares A's eigenvectors, then lambda_j = v_j^dag A v_j.  MatrixILog's
  *     result, sum_j v_j (i c arg lambda_j) v_j^dag, does not depend on the
@@ -38,6 +42,9 @@
 
 #include <cstdint>
 #include <cstdio>
+#include <cstdlib>
+#include <dlfcn.h>
+#include <string>
 
 #include "SUNc/Definitions.cpp"
 #include "orc_philox.h"
@@ -109,8 +116,37 @@ static void shim_jacobi_hermitian(COMPLEX H[9], COMPLEX W[9]) {
             }
     }
 }
-extern "C" void zgeev(char const *, char const *, int *n, COMPLEX *a, int *lda, COMPLEX *w, COMPLEX *vl, int *ldvl,
-                      COMPLEX *vr, int *ldvr, COMPLEX *work, int *lwork, double *, int *info) {
+/* LAPACK's ZGEEV with gfortran's hidden CHARACTER lengths after the arguments. */
+typedef void (*shim_zgeev_fn)(char const *, char const *, int *, COMPLEX *, int *, COMPLEX *, COMPLEX *, int *,
+                              COMPLEX *, int *, COMPLEX *, int *, double *, int *, size_t, size_t);
+
+/* The ZGEEV of the library TCYM_REF_LAPACK names at this call, or null (unset or empty:
+ * the restatement; the library or its symbol not found: a message on stderr and the
+ * restatement).  The variable is read on every call, so one process can run both. */
+static shim_zgeev_fn shim_lapack_zgeev() {
+    static std::string resolved_path;
+    static shim_zgeev_fn fn = nullptr;
+    const char *path = std::getenv("TCYM_REF_LAPACK");
+    if (!path || !*path) return nullptr;
+    if (resolved_path == path) return fn;
+    resolved_path = path;
+    fn = nullptr;
+    if (void *h = dlopen(path, RTLD_NOW | RTLD_LOCAL)) {
+        fn = (shim_zgeev_fn)dlsym(h, "zgeev_");
+        if (!fn) fn = (shim_zgeev_fn)dlsym(h, "scipy_zgeev_");
+    }
+    if (!fn) std::fprintf(stderr, "oracle: no ZGEEV in TCYM_REF_LAPACK=%s; using the restatement\n", path);
+    return fn;
+}
+
+extern "C" int ref_lapack_in_use() { return shim_lapack_zgeev() != nullptr; }
+
+extern "C" void zgeev(char const *jobvl, char const *jobvr, int *n, COMPLEX *a, int *lda, COMPLEX *w, COMPLEX *vl,
+                      int *ldvl, COMPLEX *vr, int *ldvr, COMPLEX *work, int *lwork, double *rwork, int *info) {
+    if (shim_zgeev_fn fn = shim_lapack_zgeev()) {
+        fn(jobvl, jobvr, n, a, lda, w, vl, ldvl, vr, ldvr, work, lwork, rwork, info, 1, 1);
+        return;
+    }
     if (*lwork == -1) {  // workspace query
         work[0] = COMPLEX(1.0, 0.0);
         *info = 0;

@@ -28,8 +28,10 @@ CUDA library draws); every output below is produced by the reference itself:
                            restored); Start, then 3 x (20 leapfrog steps at dt
                            0.05, Update(1)) with 16 cooling steps of sqrt_dctau
                            sqrt(0.02): the cumulative DeltaNCsCoolRealTime after
-                           each update and the cooled links (SU(3) measurements
-                           need LAPACK zgeev, absent here)
+                           each update and the cooled links
+  ref_cooling_su3.npz      the same for SU(3) at blocking levels 0 (6^3) and 1
+                           (8^3), the reference's MatrixILog calling LAPACK's ZGEEV
+                           from the OpenBLAS that SciPy ships (key "zgeev" names it)
   ref_cooling_su2_96.npz   the SU(2) 96^3 gradient-flow cooling run: U = 1, E ~
                            N(0, 1/2) (seed 4) restored by the reference, 2000
                            leapfrog steps of dt 0.05 by the reference, then 500
@@ -179,10 +181,16 @@ def cooling():
 
 
 def cooling_su3():
-    """SU(3) CoolingMethod, the reference's own (its matrix log reaching the oracle's zgeev
-    restatement): cumulative cooled ΔN_CS and cooled links, level 0 at 6^3, level 1 at 8^3."""
+    """SU(3) CoolingMethod, the reference's own, its matrix log calling LAPACK's ZGEEV in the
+    OpenBLAS that SciPy ships (the restatement in oracle/ref_wrap.cpp where that is absent;
+    the fixture records which): cumulative cooled ΔN_CS and cooled links, level 0 at 6^3,
+    level 1 at 8^3."""
+    lapack = oracle.scipy_lapack()
+    if lapack:
+        os.environ["TCYM_REF_LAPACK"] = lapack[0]
     P, R = oracle.Port(3), oracle.Ref(3)
-    out = {"dt": 0.05, "every": 20, "sqrt_dctau": np.sqrt(0.02)}
+    out = {"dt": 0.05, "every": 20, "sqrt_dctau": np.sqrt(0.02),
+           "zgeev": lapack[1] if lapack and R.lapack_in_use() else "restated (oracle/ref_wrap.cpp)"}
     for level, shape, steps, bf in ((0, (6, 6, 6), 16, 8), (1, (8, 8, 8), 12, 2)):
         U, E = oracle.empty_fields(3, shape)
         P.random_links(shape, U, 0.4, 7 + level)
@@ -199,6 +207,7 @@ def cooling_su3():
             cooled.append(R.cooling_links(level))
         out.update({f"U0_{level}": U, f"E0_{level}": E, f"totals{level}": np.array(totals),
                     f"cooled{level}": np.array(cooled), f"steps{level}": steps, f"bf{level}": bf})
+    os.environ.pop("TCYM_REF_LAPACK", None)
     np.savez_compressed(os.path.join(HERE, "ref_cooling_su3.npz"), **out)
 
 

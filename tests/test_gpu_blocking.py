@@ -94,8 +94,9 @@ def test_blocked_cooling_matches_reference(ctx, prec, level):
 
 @pytest.mark.parametrize("prec", PREC)
 def test_blocked_cooling_su3_matches_oracle(ctx, oracle_port, prec):
-    """SU(3) 8^3 at StandardBlockingLevel 1 (the reference's SU(3) log needs LAPACK):
-    the device's cooled links and Delta N_CS against the oracle's blocked cooling."""
+    """SU(3) 8^3 at StandardBlockingLevel 1: the device's cooled links and Delta N_CS
+    against the oracle's blocked cooling (the oracle equals the reference's own, run on
+    LAPACK's ZGEEV, in the golden tests)."""
     P = oracle_port[3]
     shape = (8, 8, 8)
     U, E = oracle.empty_fields(3, shape)

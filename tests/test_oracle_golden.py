@@ -227,8 +227,8 @@ def test_block_is_the_product_of_two_links(oracle_port):
 @pytest.mark.parametrize("level", [0, 1])
 def test_su3_cooling_equals_reference(oracle_port, level):
     """SU(3) CoolingMethod (level 0 at 6^3, blocking level 1 at 8^3), the reference's own
-    with LAPACK's zgeev restated (its only use: the eigensystem of a unitary 3x3 in
-    MatrixILog): the oracle's cooled links and cumulative cooled Delta N_CS equal it."""
+    with its MatrixILog calling LAPACK's ZGEEV (OpenBLAS 0.3.31 as SciPy ships it): the
+    oracle's cooled links and cumulative cooled Delta N_CS equal it."""
     d = load("ref_cooling_su3.npz")
     P = oracle_port[3]
     U, E = d[f"U0_{level}"].copy(), d[f"E0_{level}"].copy()
@@ -246,13 +246,23 @@ def test_su3_cooling_equals_reference(oracle_port, level):
         old = new
 
 
-def test_su3_matrix_log_equals_reference(oracle_port):
-    """The reference's SU(3) MatrixILog (zgeev restated) against the oracle's log on
-    elements up to and across the branch cut at angle pi."""
+@pytest.mark.parametrize("zgeev", ["restated", "lapack"])
+def test_su3_matrix_log_equals_reference(oracle_port, monkeypatch, zgeev):
+    """The reference's SU(3) MatrixILog, its ZGEEV either restated or LAPACK's (SciPy's
+    OpenBLAS), against the oracle's log on elements up to and across the branch cut at
+    angle pi."""
     if not oracle.ref_available(3):
         pytest.skip("the reference's sources are compiled only where they are present")
     R = oracle.Ref(3)
     P = oracle_port[3]
+    if zgeev == "lapack":
+        lapack = oracle.scipy_lapack()
+        if lapack is None:
+            pytest.skip("no LAPACK with ZGEEV found")
+        monkeypatch.setenv("TCYM_REF_LAPACK", lapack[0])
+    else:
+        monkeypatch.delenv("TCYM_REF_LAPACK", raising=False)
+    assert R.lapack_in_use() == (zgeev == "lapack")
     rng = np.random.default_rng(3)
     for scale in (1e-3, 0.1, 1.0, 3.0):
         for _ in range(10):
