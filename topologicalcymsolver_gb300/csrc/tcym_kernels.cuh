@@ -63,6 +63,49 @@ constexpr int kThreadsPair = 128;
 template <int FMT> constexpr int pair_min_blocks_for() {
     return Fmt<FMT>::NA == 8 ? TCYM_SU3_PAIR_MINBLOCKS : TCYM_SU2_PAIR_MINBLOCKS;
 }
+// L2 prefetch at the start of a block of the linear paired step: bit 0 the
+// block's own field lines, bit 1 the lines of U_0, U_1 one pair-plane up in z
+#ifndef TCYM_PAIR_PREFETCH
+#define TCYM_PAIR_PREFETCH 0
+#endif
+
+// The lines a block of the linear paired step (pairs [p0, p0 + kThreadsPair))
+// reads first from DRAM: its own fields, loaded only when each direction's
+// update needs them, and the links U_0, U_1 of the pairs one step up in z,
+// which its plaquettes read before the block owning them runs.  Each thread
+// issues a few L2 prefetches (hints: no registers held, nothing waits on them),
+// all inside the field and link arrays.  Planes: SU(3) FP32 links 6 x 16 B per
+// pair and direction, fields 4 x 16 B; SU(2) FP32 links 2 x 16 B, fields 3 x 8 B.
+template <int FMT>
+__device__ __forceinline__ void prefetch_pair_block(const Geom &g, const void *Uin, const void *E, int64_t p0, int what) {
+    constexpr bool su3 = Fmt<FMT>::NA == 8;
+    constexpr int LP = su3 ? 6 : 2, LB = 16;   // link planes per direction, bytes per pair
+    constexpr int EP = su3 ? 4 : 3, EB = su3 ? 16 : 8;
+    constexpr int e_lines = 3 * EP * (kThreadsPair * EB / 128);
+    constexpr int z_lines = 2 * LP * (kThreadsPair * LB / 128);
+    const int64_t Vh = g.V >> 1;
+    const int64_t sz = (int64_t)g.nx * g.ny;
+    int64_t pz = p0 + sz;  // one pair-plane up; from the last plane, the seam's partner plane 0
+    if (pz >= Vh) pz -= Vh;
+    for (int i = threadIdx.x; i < e_lines + z_lines; i += kThreadsPair) {
+        const char *addr = nullptr;
+        if (i < e_lines) {
+            if (!(what & 1)) continue;
+            constexpr int per = kThreadsPair * EB / 128;
+            const int plane = i / per;
+            const int64_t q = p0 + (int64_t)(i % per) * (128 / EB);
+            if (q < Vh) addr = static_cast<const char *>(E) + ((int64_t)plane * Vh + q) * EB;
+        } else {
+            if (!(what & 2)) continue;
+            constexpr int per = kThreadsPair * LB / 128;
+            const int j = i - e_lines;
+            const int plane = j / per;  // direction plane / LP, component plane % LP
+            const int64_t q = pz + (int64_t)(j % per) * (128 / LB);
+            if (q < Vh) addr = static_cast<const char *>(Uin) + ((int64_t)plane * Vh + q) * LB;
+        }
+        if (addr) asm volatile("prefetch.global.L2 [%0];" ::"l"(addr));
+    }
+}
 
 inline int grid_for(int64_t n, int threads) {
     int64_t b = (n + threads - 1) / threads;
@@ -110,6 +153,7 @@ __global__ void __launch_bounds__(kThreadsPair, pair_min_blocks_for<FMT>())
         if (!tile_pair(g, t, blockIdx.x, threadIdx.x, p, seam)) return;
     } else {
         const int64_t p0 = ((int64_t)blockIdx.x + t.b0) * kThreadsPair;
+        if (TCYM_PAIR_PREFETCH) prefetch_pair_block<FMT>(g, Uin, E, p0, TCYM_PAIR_PREFETCH);
         p = p0 + threadIdx.x;
         if (p >= (g.V >> 1)) return;
         seam = pairs_touch_seam(g, p0, kThreadsPair);
