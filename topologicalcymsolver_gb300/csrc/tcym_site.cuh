@@ -199,6 +199,11 @@ TCYM_COLD void langevin_kick_pair(const StepCoef<float> &c, int mu, int64_t p, i
 // The plaquette form (see plaquette_projections) took the SU(3) step from
 // 0.366 to 0.331 ms per 128^3 step on GB300 and, needing fewer registers,
 // runs 4 blocks of 128 per SM without spills (the staple form: 3).
+// 1: the two lower staples of a direction in a rolled loop (half the code of
+// the direction's phase), 0: unrolled
+#ifndef TCYM_PAIR_STAPLE_ROLLED
+#define TCYM_PAIR_STAPLE_ROLLED 0
+#endif
 template <class F, bool SEAM, int MODE = -1>
 TCYM_HD void site_step_pair(const Geom &g, const void *Uin, void *Uout, void *E, const StepCoef<float> &c,
                             const StepCoef<float> &cn, int64_t p, uint64_t step_add, f2 *sm, int stride) {
@@ -215,7 +220,11 @@ TCYM_HD void site_step_pair(const Geom &g, const void *Uin, void *Uout, void *E,
     for (int mu = 0; mu < 3; ++mu) {
         // lower staples S- = U_nu^dag(x+mu-nu) U_mu^dag(x-nu) U_nu(x-nu)
         M2 A = G2::zero();
+#if TCYM_PAIR_STAPLE_ROLLED
+#pragma unroll 1
+#else
 #pragma unroll
+#endif
         for (int k = 1; k <= 2; ++k) {
             const int nu = mu + k >= 3 ? mu + k - 3 : mu + k;
             const M2 b1 = F::load2(Uin, Vh, nu, nb.at(mu, 1, nu, -1), SEAM && nb.swapped(mu, 1, nu, -1));
