@@ -144,8 +144,9 @@ def test_energy_drift_1e4_steps_at_128_fp32(ctx):
     """The FP32-storage step holds |dE/E| <= 1e-6 over 10^4 steps at 128^3 to the
     resolution the fluctuating energy allows: over four starts, the halves of each run
     differ by a few 1e-6 with either sign (the leapfrog energy's fluctuation at this
-    volume; measured -2.0e-6 .. 1.6e-6, and -1.9e-6 .. 1.3e-6 for the previous staple
-    form of the step) and their mean is within 2e-6 of zero."""
+    volume, a half's mean carrying a standard error near 0.9e-6; measured -3.1e-6 ..
+    1.6e-6 over eight starts, and -1.9e-6 .. 1.3e-6 for the previous staple form of the
+    step) and their mean is within 2e-6 of zero."""
     runs = [_drift(ctx, tcym.FP32, seed) for seed in range(4)]
     halves = np.array([h for h, _ in runs])
     fits = np.array([f for _, f in runs])
