@@ -404,6 +404,17 @@ int tcym_server_stats(tcym_server srv, tcym_server_info *out);
  * ensemble's stride steps and the N_CS sample) and how many requests were being
  * prepared when it started (either array may be NULL); *n = ticks returned. */
 int tcym_server_ticks(tcym_server srv, double *ms, double *preparing, int capacity, int *n);
+/* One tick of the request loop. */
+typedef struct {
+    double ms;           /* the tick: stride steps of every running request and their N_CS samples */
+    double gap_ms;       /* from the end of the previous tick to the start of this one (joins of prepared
+                            requests, retirements, the ensemble's re-capture when its members changed) */
+    double link_updates; /* link-updates the tick advanced */
+    int active;          /* running requests */
+    int preparing;       /* requests being prepared when it started */
+} tcym_tick;
+/* The same last (up to `capacity`) ticks as full records, oldest first. */
+int tcym_server_tick_log(tcym_server srv, tcym_tick *ticks, int capacity, int *n);
 
 #ifdef __cplusplus
 }

@@ -179,6 +179,32 @@ def test_gauss_restore(ctx, oracle_port, nc):
     assert o[9] <= 1e-13 and o[15] < 1e-12
 
 
+@pytest.mark.parametrize("shape", [(6, 6, 6), (5, 6, 7)], ids=["paired", "odd_nz"])
+@pytest.mark.parametrize("nc", GROUPS)
+def test_gauss_restore_fp32_against_oracle(ctx, oracle_port, nc, shape):
+    """FP32 storage: 8 restore iterations (tol 0, so both run them all; the absolute
+    maximum falls from ~5 to ~5e-4) against the FP64 oracle's from the same state.  Even
+    nz takes the paired FP32 kernels (packed pairs, FP32 arithmetic and scratch), odd nz
+    the per-site kernels (FP64 accumulation): the fields within 1e-5 of their scale, the
+    restored state's violation (signed max and absolute max) within 1e-5 of the oracle's."""
+    P = oracle_port[nc]
+    U, E = random_state(P, nc, shape, seed=57)
+    lat = tcym.Lattice(ctx, nc, shape, tcym.FP32)
+    lat.upload(U, E)
+    it_g, _ = lat.gauss_restore(0.0, 8)
+    it_o = P.gauss_restore(shape, U, E, 0.0, 8)
+    Ug, Eg = lat.download()
+    err = rel(Eg, E)
+    o = P.observables(shape, U, E)
+    og = lat.observables()
+    dg = max(abs(og.gauss_max - o[9]), abs(og.gauss_absmax - o[15]))
+    print(f"\nmeasured FP32 restore SU({nc}) {shape}: E {err:.2e}, violation {dg:.2e} of {o[15]:.3e}")
+    assert it_g == 8 and it_o == 8
+    assert err < 1e-5
+    assert dg < 1e-5 * max(1.0, abs(o[15]))
+    lat.close()
+
+
 @pytest.mark.parametrize("prec", PREC)
 @pytest.mark.parametrize("nc", GROUPS)
 def test_gauss_restore_reports_nan(ctx, oracle_port, nc, prec):

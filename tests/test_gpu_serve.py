@@ -127,6 +127,12 @@ def test_ticks_continue_while_a_large_request_is_prepared(ctx):
     assert len(during) >= 5
     assert np.median(during) < 4.0 * base + 1.0
     assert during.max() < 0.5 * 1e3 * st["prep_seconds"]  # no tick waited for the whole preparation
+    # the full records: each tick's work and the time between ticks
+    log = s.tick_log()
+    assert len(log) > 0 and np.all(log["ms"] > 0)
+    assert np.all(log["active"] >= 1) and np.all(log["gap_ms"] >= 0)
+    small_work = 3 * 16 ** 3 * 20  # one 16^3 request's stride of 20 steps
+    assert np.all(log["link_updates"] >= small_work)
     for rid in small:
         assert s.status(rid)[0] == tcym.REQ_RUNNING
     s.close()  # abandons the small requests

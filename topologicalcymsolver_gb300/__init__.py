@@ -90,6 +90,10 @@ class _ServerInfo(ctypes.Structure):
 
 _LIB = None
 _dp = ctypes.POINTER(ctypes.c_double)
+# tcym_tick: three doubles, two ints, padded to 32 bytes
+TICK_DTYPE = np.dtype({"names": ["ms", "gap_ms", "link_updates", "active", "preparing"],
+                       "formats": [np.float64, np.float64, np.float64, np.int32, np.int32],
+                       "offsets": [0, 8, 16, 24, 28], "itemsize": 32})
 
 
 def library() -> ctypes.CDLL:
@@ -192,6 +196,8 @@ def library() -> ctypes.CDLL:
                                 _dp], ctypes.c_int),
         "tcym_server_stats": ([ctypes.c_void_p, ctypes.POINTER(_ServerInfo)], ctypes.c_int),
         "tcym_server_ticks": ([ctypes.c_void_p, _dp, _dp, ctypes.c_int, ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
+        "tcym_server_tick_log": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int)],
+                                 ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -652,6 +658,15 @@ class Server:
         self.ctx.check(self.lib.tcym_server_ticks(self.h, ms.ctypes.data_as(_dp), prep.ctypes.data_as(_dp), capacity,
                                                   ctypes.byref(n)))
         return ms[: n.value], prep[: n.value]
+
+    def tick_log(self, capacity: int = 8192) -> np.ndarray:
+        """The last ticks as a structured array (ms, gap_ms, link_updates, active, preparing),
+        oldest first (tcym_tick)."""
+        rec = np.zeros(capacity, dtype=TICK_DTYPE)
+        n = ctypes.c_int()
+        self.ctx.check(self.lib.tcym_server_tick_log(self.h, rec.ctypes.data_as(ctypes.c_void_p), capacity,
+                                                     ctypes.byref(n)))
+        return rec[: n.value]
 
     def close(self):
         if self.h:

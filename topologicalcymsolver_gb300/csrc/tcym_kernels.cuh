@@ -293,6 +293,95 @@ __global__ void __launch_bounds__(threads_for<FMT>()) k_gauss_update_it(Geom g, 
     site_gauss_update<Fmt<FMT>>(g, U, E, G, gam, s);
 }
 
+// The restore iteration for the FP32 formats with even nz: one thread per site
+// pair in packed FP32, G(x) kept as FP32 pair planes G2[a * Vh + p] (the
+// storage's precision; the scratch holds na * V doubles, twice what they need).
+// The per-site sums run in FP32 per thread and the block partials in FP64,
+// with the same signed maximum (fmax drops NaN; the sums keep it).
+TCYM_HD f2 swap_f2(f2 v) { return f2(v.v.y, v.v.x); }
+// 0: the FP32 formats restore through the per-site kernels too
+#ifndef TCYM_RESTORE_PAIRED
+#define TCYM_RESTORE_PAIRED 1
+#endif
+
+template <int FMT>
+__global__ void __launch_bounds__(kRedThreads) k_gauss_compute_pair_it(Geom g, const void *U, const void *E, f2 *G2,
+                                                                       double *partial, const double *ctl, int it) {
+    if ((double)it >= ctl[0]) return;
+    using F = Fmt<FMT>;
+    using GG = typename F::G2;
+    constexpr int NA = F::NA;
+    const int64_t Vh = g.V >> 1;
+    float gsq = 0.f, gmax = 0.f, gabs = 0.f;
+    for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < Vh; p += (int64_t)gridDim.x * blockDim.x) {
+        const PairNbhd nb(g, p);
+        f2 gv[NA];
+#pragma unroll
+        for (int a = 0; a < NA; ++a) gv[a] = f2(0.0);
+#pragma unroll 1
+        for (int mu = 0; mu < 3; ++mu) {
+            const int64_t pm = nb.at(mu, -1);
+            const bool sw = nb.swapped(mu, -1);
+            f2 e[NA], em[NA], t[NA];
+            F::load_e2(E, Vh, mu, pm, em);
+            if (sw) {
+#pragma unroll
+                for (int a = 0; a < NA; ++a) em[a] = swap_f2(em[a]);
+            }
+            GG::inverse_adjoint(F::load2(U, Vh, mu, pm, sw), em, t);
+            F::load_e2(E, Vh, mu, p, e);
+#pragma unroll
+            for (int a = 0; a < NA; ++a) gv[a] += e[a] - t[a];
+        }
+#pragma unroll
+        for (int a = 0; a < NA; ++a) {
+            G2[a * Vh + p] = gv[a];
+            const float x = gv[a].v.x, y = gv[a].v.y;
+            gsq = fmaf(x, x, fmaf(y, y, gsq));
+            gmax = fmaxf(gmax, fmaxf(x, y));
+            gabs = fmaxf(gabs, fmaxf(fabsf(x), fabsf(y)));
+        }
+    }
+    double v[P_WIDTH];
+#pragma unroll
+    for (int k = 0; k < P_WIDTH; ++k) v[k] = 0.0;
+    v[P_GSQ] = gsq;
+    v[P_GMAX] = gmax;
+    v[P_GABS] = gabs;
+    block_partial(v, partial);
+}
+
+// E_mu(x) -= gam (G(x) - U_mu(x) G(x+mu) U_mu^dag(x)) for both sites of a pair, in FP32
+template <int FMT>
+__global__ void __launch_bounds__(kThreadsPair) k_gauss_update_pair_it(Geom g, const void *U, void *E, const f2 *G2,
+                                                                      float gam, const double *ctl, int it) {
+    if ((double)it >= ctl[0]) return;
+    using F = Fmt<FMT>;
+    using GG = typename F::G2;
+    constexpr int NA = F::NA;
+    const int64_t Vh = g.V >> 1;
+    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= Vh) return;
+    const PairNbhd nb(g, p);
+    const f2 mg(-(double)gam);
+    f2 gx[NA];
+#pragma unroll
+    for (int a = 0; a < NA; ++a) gx[a] = G2[a * Vh + p];
+#pragma unroll 1
+    for (int mu = 0; mu < 3; ++mu) {
+        const int64_t pp = nb.at(mu, 1);
+        const bool sw = nb.swapped(mu, 1);
+        f2 gp[NA], t[NA], e[NA];
+#pragma unroll
+        for (int a = 0; a < NA; ++a) gp[a] = sw ? swap_f2(G2[a * Vh + pp]) : G2[a * Vh + pp];
+        GG::adjoint(F::load2(U, Vh, mu, p, false), gp, t);
+        F::load_e2(E, Vh, mu, p, e);
+#pragma unroll
+        for (int a = 0; a < NA; ++a) e[a] = fma(mg, gx[a] - t[a], e[a]);
+        F::store_e2(E, Vh, mu, p, e);
+    }
+}
+
 template <int FMT> __global__ void k_set_zero(Geom g, void *U, void *E) {
     int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (s < g.V) site_set_zero<Fmt<FMT>>(g, U, E, s);
@@ -434,13 +523,29 @@ template <int FMT> struct Launch {
         k_gauss_update<FMT><<<grid_for(g.V, TPB), TPB, 0, st>>>(g, U, E, G, gam);
         return cudaGetLastError();
     }
+    // the restore iteration: paired FP32 kernels where the storage is paired
+    static constexpr bool restore_paired(const Geom &g) { return TCYM_RESTORE_PAIRED && Fmt<FMT>::PAIRED && g.nz % 2 == 0; }
     static cudaError_t gauss_compute_it(const Geom &g, const void *U, const void *E, double *G, double *partial,
                                         int blocks, const double *ctl, int it, cudaStream_t st) {
+        if constexpr (Fmt<FMT>::PAIRED) {
+            if (restore_paired(g)) {
+                k_gauss_compute_pair_it<FMT><<<blocks, kRedThreads, 0, st>>>(g, U, E, reinterpret_cast<f2 *>(G),
+                                                                             partial, ctl, it);
+                return cudaGetLastError();
+            }
+        }
         k_gauss_compute_it<FMT><<<blocks, kRedThreads, 0, st>>>(g, U, E, G, partial, ctl, it);
         return cudaGetLastError();
     }
     static cudaError_t gauss_update_it(const Geom &g, const void *U, void *E, const double *G, double gam,
                                        const double *ctl, int it, cudaStream_t st) {
+        if constexpr (Fmt<FMT>::PAIRED) {
+            if (restore_paired(g)) {
+                k_gauss_update_pair_it<FMT><<<grid_for(g.V >> 1, kThreadsPair), kThreadsPair, 0, st>>>(
+                    g, U, E, reinterpret_cast<const f2 *>(G), (float)gam, ctl, it);
+                return cudaGetLastError();
+            }
+        }
         k_gauss_update_it<FMT><<<grid_for(g.V, TPB), TPB, 0, st>>>(g, U, E, G, gam, ctl, it);
         return cudaGetLastError();
     }

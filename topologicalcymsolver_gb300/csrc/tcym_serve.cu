@@ -95,7 +95,8 @@ struct tcym_server_s {
     double link_updates = 0.0;
     uint64_t completed = 0, failed = 0, ticks = 0;
     double prep_seconds = 0.0;
-    std::vector<double> tick_ms, tick_prep;  // per tick: duration, preparations under way at its start
+    std::vector<tcym_tick> tick_log;  // the last ticks (at most kTickRecord)
+    Clock::time_point last_tick_end{};
     int loop_error = TCYM_OK;
 };
 
@@ -194,21 +195,27 @@ void tick_loop(tcym_server srv) {
         }
         // one tick: every active request advances `stride` steps and is sampled
         const int n = (int)srv->active.size();
-        const int preparing = srv->preparing;
+        tcym_tick rec{};
+        rec.active = n;
+        rec.preparing = srv->preparing;
+        for (uint64_t id : srv->active) {
+            const tcym_request &q = srv->reqs[id].spec;
+            rec.link_updates += 3.0 * (double)q.L * q.L * q.L * srv->stride;
+        }
         std::vector<double> ncs(n), edb(n);
         lk.unlock();
         const auto t0 = Clock::now();
         int rc = tcym_ensemble_step(srv->ens, srv->stride);
         if (!rc) rc = tcym_ensemble_measure(srv->ens, srv->stride, edb.data(), ncs.data());
-        const double ms = std::chrono::duration<double, std::milli>(Clock::now() - t0).count();
+        const auto t1 = Clock::now();
+        rec.ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
         lk.lock();
+        rec.gap_ms = srv->ticks ? std::chrono::duration<double, std::milli>(t0 - srv->last_tick_end).count() : 0.0;
+        srv->last_tick_end = t1;
         ++srv->ticks;
-        if (srv->tick_ms.size() >= kTickRecord) {
-            srv->tick_ms.erase(srv->tick_ms.begin(), srv->tick_ms.begin() + kTickRecord / 2);
-            srv->tick_prep.erase(srv->tick_prep.begin(), srv->tick_prep.begin() + kTickRecord / 2);
-        }
-        srv->tick_ms.push_back(ms);
-        srv->tick_prep.push_back((double)preparing);
+        if (srv->tick_log.size() >= kTickRecord)
+            srv->tick_log.erase(srv->tick_log.begin(), srv->tick_log.begin() + kTickRecord / 2);
+        srv->tick_log.push_back(rec);
         if (rc) {  // a device failure ends the loop; every pending request fails
             srv->loop_error = rc;
             for (uint64_t id : srv->active) retire(srv, srv->reqs[id], TCYM_REQ_FAILED, true);
@@ -393,12 +400,22 @@ extern "C" int tcym_server_stats(tcym_server srv, tcym_server_info *out) {
 extern "C" int tcym_server_ticks(tcym_server srv, double *ms, double *preparing, int capacity, int *n) {
     if (!srv || capacity < 0) return TCYM_ERR_ARG;
     std::lock_guard<std::mutex> g(srv->mu);
-    const int total = (int)srv->tick_ms.size();
+    const int total = (int)srv->tick_log.size();
     const int k = std::min(total, capacity);
     for (int i = 0; i < k; ++i) {
-        if (ms) ms[i] = srv->tick_ms[total - k + i];
-        if (preparing) preparing[i] = srv->tick_prep[total - k + i];
+        if (ms) ms[i] = srv->tick_log[total - k + i].ms;
+        if (preparing) preparing[i] = (double)srv->tick_log[total - k + i].preparing;
     }
+    if (n) *n = k;
+    return TCYM_OK;
+}
+
+extern "C" int tcym_server_tick_log(tcym_server srv, tcym_tick *ticks, int capacity, int *n) {
+    if (!srv || capacity < 0 || (capacity > 0 && !ticks)) return TCYM_ERR_ARG;
+    std::lock_guard<std::mutex> g(srv->mu);
+    const int total = (int)srv->tick_log.size();
+    const int k = std::min(total, capacity);
+    for (int i = 0; i < k; ++i) ticks[i] = srv->tick_log[total - k + i];
     if (n) *n = k;
     return TCYM_OK;
 }

@@ -214,6 +214,7 @@ def run_serve(a, progress=sys.stderr):
     makespan = time.perf_counter() - start
     stats = srv.stats()
     tick_ms, tick_prep = srv.ticks()
+    log = srv.tick_log()
     srv.close()
     ctx.close()
     total = sum(_work(r) for r in reqs)
@@ -234,7 +235,28 @@ def run_serve(a, progress=sys.stderr):
                     "median_idle_preparers": (float(np.median(tick_ms[tick_prep == 0]))
                                               if np.any(tick_prep == 0) else None),
                     "note": "last <= 8192 ticks; a tick = stride steps of every running request + its N_CS sample"},
+        "tick_log": _tick_summary(log),
     }
+
+
+def _tick_summary(log):
+    """Where the request loop's time went over the recorded ticks: the link-update rate
+    inside ticks, the share of wall time in ticks and between them, by preparations
+    under way and by running requests."""
+    if len(log) == 0:
+        return None
+    ms, gap, lu = log["ms"], log["gap_ms"], log["link_updates"]
+    busy = log["preparing"] > 0
+    wall = float(ms.sum() + gap.sum())
+    out = {"ticks": int(len(log)), "wall_s": wall * 1e-3,
+           "in_tick_link_updates_per_s": float(lu.sum() / ms.sum() * 1e3),
+           "share_in_ticks": float(ms.sum() / wall), "gap_ms_median": float(np.median(gap)),
+           "gap_ms_total_s": float(gap.sum() * 1e-3), "active_median": float(np.median(log["active"]))}
+    for name, sel in (("while_preparing", busy), ("preparers_idle", ~busy)):
+        if np.any(sel):
+            out[f"in_tick_link_updates_per_s_{name}"] = float(lu[sel].sum() / ms[sel].sum() * 1e3)
+            out[f"ticks_{name}"] = int(sel.sum())
+    return out
 
 
 def run(name: str, a):
