@@ -138,14 +138,34 @@ def test_su2_cooling_sweeps_against_oracle(ctx, oracle_port, prec, tol, tol_mag)
     assert all(b < a for a, b in zip(mags, mags[1:]))  # cooling lowers the magnetic energy
 
 
+def _cool_series(lat, mode, records):
+    """`records` x 10 sweeps of dtau 0.02 in `mode`: (T00, ELECTRIC, MAGNETIC, cooled N_CS so far)
+    after each 10."""
+    out, t = [], 0.0
+    for _ in range(records):
+        t += lat.flow(0.02, 10, mode, calibrate=tcym.NCS_IMPROVED)
+        o = lat.observables()
+        out.append([o.T00, o.electric, o.magnetic, t])
+    return np.array(out)
+
+
+def _series_errors(got, ref):
+    """Per record: |magnetic / reference - 1| and |N_CS - reference| over the reference's
+    largest 10-sweep N_CS increment."""
+    mag = np.abs(got[:, 2] / ref[:, 2] - 1)
+    scale = np.abs(np.diff(np.concatenate([[0.0], ref[:, 3]]))).max()
+    return mag, np.abs(got[:, 3] - ref[:, 3]) / scale
+
+
 def test_su2_96_cooling_against_reference_run(ctx):
     """The SU(2) 96^3 cooling run at full size against tests/golden/ref_cooling_su2_96.npz:
     U = 1, E ~ N(0, 1/2) (seed 4) restored as the reference restores (1e-14, at most
     10000 iterations), 2000 leapfrog steps in FP64 (the start matches the reference's
     own, sampled at 64 sites and through its observables), then 500 sweeps of dtau 0.02
-    with energy and cooled N_CS (improved E.B, trapezoid along the flow) every 10 sweeps:
-    FP32-storage checkerboard sweeps against the oracle's checkerboard series, and FP64
-    simultaneous sweeps against the reference's own CalibrationUpdate series."""
+    with energy and cooled N_CS (improved E.B, trapezoid along the flow) every 10 sweeps,
+    each flow in FP64 and in FP32 storage: checkerboard sweeps against the oracle's
+    checkerboard series, simultaneous sweeps against the reference's own CalibrationUpdate
+    series."""
     d = dict(np.load(os.path.join(G, "ref_cooling_su2_96.npz")))
     shape = (96, 96, 96)
     l64 = tcym.Lattice(ctx, 2, shape, tcym.FP64)
@@ -158,32 +178,30 @@ def test_su2_96_cooling_against_reference_run(ctx):
     fp_u, fp_e = rel(U[idx], d["fp_U"]), rel(E[idx], d["fp_E"])
     o = l64.observables().as_oracle_vector()
     fp_t = abs(o[0] / d["start_obs"][0] - 1)
-    l32 = tcym.Lattice(ctx, 2, shape, tcym.FP32)
-    l32.copy_from(l64)
-    cb, sim = d["checkerboard"], d["simultaneous"]
-    got32, got64, t32, t64 = [], [], 0.0, 0.0
-    for _ in range(len(cb)):
-        t32 += l32.flow(0.02, 10, tcym.FLOW_CHECKERBOARD, calibrate=tcym.NCS_IMPROVED)
-        t64 += l64.flow(0.02, 10, tcym.FLOW_SIMULTANEOUS, calibrate=tcym.NCS_IMPROVED)
-        a, b = l32.observables(), l64.observables()
-        got32.append([a.T00, a.electric, a.magnetic, t32])
-        got64.append([b.T00, b.electric, b.magnetic, t64])
-    got32, got64 = np.array(got32), np.array(got64)
-    mag32 = np.abs(got32[:, 2] / cb[:, 2] - 1)
-    mag64 = np.abs(got64[:, 2] / sim[:, 2] - 1)
-    dscale = np.abs(np.diff(np.concatenate([[0.0], cb[:, 3]]))).max()  # the largest 10-sweep increment
-    ncs32 = np.abs(got32[:, 3] - cb[:, 3]) / dscale
-    ncs64 = np.abs(got64[:, 3] - sim[:, 3]) / np.abs(np.diff(np.concatenate([[0.0], sim[:, 3]]))).max()
-    print(f"\nmeasured SU(2) 96^3 cooling: start U {fp_u:.2e} E {fp_e:.2e} T00 {fp_t:.2e}; FP32 checkerboard "
-          f"magnetic {mag32[:3].max():.2e} (30 sweeps) {mag32.max():.2e} (500), N_CS {ncs32[:3].max():.2e} / "
-          f"{ncs32.max():.2e}; FP64 simultaneous magnetic {mag64[:3].max():.2e} / {mag64.max():.2e}, N_CS "
-          f"{ncs64[:3].max():.2e} / {ncs64.max():.2e}")
+    print(f"\nmeasured SU(2) 96^3 cooling start: U {fp_u:.2e} E {fp_e:.2e} T00 {fp_t:.2e}")
     assert fp_u < 1e-9 and fp_e < 1e-9 and fp_t < 1e-10
-    assert np.all(np.diff(got32[:, 2]) < 0) and np.all(np.diff(got64[:, 2]) < 0)  # cooling lowers B^2
-    assert mag32[:3].max() < 1e-5 and ncs32[:3].max() < 1e-5
-    assert mag64[:3].max() < 1e-9 and ncs64[:3].max() < 1e-9
-    assert mag32.max() < 1e-3 and ncs32.max() < 1e-3
-    assert mag64.max() < 1e-6 and ncs64.max() < 1e-6
+    n = len(d["checkerboard"])
+    runs = {}
+    for prec in (tcym.FP64, tcym.FP32):
+        for mode, key in ((tcym.FLOW_CHECKERBOARD, "checkerboard"), (tcym.FLOW_SIMULTANEOUS, "simultaneous")):
+            lat = tcym.Lattice(ctx, 2, shape, prec)
+            lat.copy_from(l64)
+            got = _cool_series(lat, mode, n)
+            unit = lat.observables().unit_max
+            lat.close()
+            mag, ncs = _series_errors(got, d[key])
+            name = f"{'FP64' if prec == tcym.FP64 else 'FP32'} {key}"
+            runs[name] = (got, mag, ncs)
+            print(f"measured SU(2) 96^3 cooling {name}: magnetic {mag[:3].max():.2e} (30 sweeps) "
+                  f"{mag.max():.2e} (500), N_CS {ncs[:3].max():.2e} / {ncs.max():.2e}; unitarity {unit:.1e}")
+            print("  magnetic per record " + " ".join(f"{x:.1e}" for x in mag))
+            print("  N_CS per record     " + " ".join(f"{x:.1e}" for x in ncs))
+    for name, (got, mag, ncs) in runs.items():
+        assert np.all(np.diff(got[:, 2]) < 0), name  # cooling lowers B^2
+        if name.startswith("FP64"):
+            assert mag.max() < 1e-6 and ncs.max() < 1e-6, name
+        else:
+            assert mag[:3].max() < 1e-5 and ncs[:3].max() < 1e-5, name
 
 
 def test_energy_drift_fp32_vs_fp64(ctx):

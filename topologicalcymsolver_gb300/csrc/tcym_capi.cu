@@ -923,6 +923,10 @@ extern "C" int tcym_flow(tcym_lattice lat, double dtau, int nsteps, int mode, in
                 for (int mu = 0; mu < 3; ++mu)
                     DISPATCH(lat->fmt, CK(L::flow_cb(lat->g, lat->U[lat->cur], p, mu, c.fc, c.cnu, c.uc, lat->stream)));
         }
+        // FP32 storage: every sweep ends on the group (FP32 renormalisation), so that
+        // rounding does not accumulate into the links over a long flow
+        if (lat->precision == TCYM_FP32)
+            DISPATCH(lat->fmt, CK(L::renormalize(lat->g, lat->U[lat->cur], lat->stream)));
         if (calibrate) {
             if ((r = tcym_reduce(lat, op, 0.0))) return r;
             if ((r = fetch_result(lat))) return r;
