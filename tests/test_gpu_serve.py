@@ -8,14 +8,17 @@
 * failures are handled on the host: a bounded wait times out, and a request
   whose initial fields are NaN (fault injected through its parameters) fails
   alone while the others complete;
-* a request's preparation (initial fields and their FP64 Gauss restore) runs on
-  its own threads and streams: the running requests keep ticking meanwhile.
+* a request's preparation (initial fields and their Gauss restore in the
+  request's precision) runs on its own threads and streams: the running requests
+  keep ticking meanwhile;
+* a served request's N_CS series equals the oracle's run of the same trajectory.
 """
 import time
 
 import numpy as np
 import pytest
 
+import oracle
 import topologicalcymsolver_gb300 as tcym
 
 pytestmark = pytest.mark.gpu
@@ -69,6 +72,41 @@ def test_series_equals_lattice_path(ctx):
     assert np.allclose(series[:, 0], [stride * (k + 1) for k in range(n // stride)])
     assert np.allclose(series[:, 1], ref, rtol=1e-9, atol=1e-12)
     assert latency > 0
+
+
+@pytest.mark.parametrize("prec", [tcym.FP64, tcym.FP32], ids=["fp64", "fp32"])
+def test_served_request_against_oracle(ctx, oracle_port, prec):
+    """An SU(3) 6^3 leapfrog request served beside two others, against the oracle run of
+    the same trajectory: U = 1, E ~ N(0, T) from the request's Philox stream, Gauss
+    restored as the server restores (FP64: 1e-12, FP32: 1e-6, at most 400 iterations),
+    then strides of 20 steps with N_CS += dt * 20 * (clover E.B) / 8 pi^2 after each.
+    FP64 within 1e-9 of the series' scale, FP32 within 1e-5."""
+    nc, L, T, n, stride, dt, seed = 3, 6, 0.7, 60, 20, 0.05, 41
+    s = tcym.Server(ctx, 2 * GB, stride=stride)
+    others = [s.submit(nc=2, L=8, T=0.5, nsteps=100, seed=1), s.submit(nc=3, L=4, T=0.9, nsteps=40, seed=2)]
+    rid = s.submit(nc=nc, L=L, T=T, nsteps=n, dynamics=tcym.DYN_LEAPFROG, dt=dt, precision=prec, seed=seed)
+    assert s.wait(rid, 300) == 0
+    series, _, rc = s.result(rid)
+    for o in others:
+        assert s.wait(o, 300) == 0
+    s.close()
+    P = oracle_port[nc]
+    shape = (L, L, L)
+    U, E = oracle.empty_fields(nc, shape)
+    P.set_zero(shape, U, E)
+    P.gaussian_efield(shape, E, np.sqrt(T), seed)
+    P.gauss_restore(shape, U, E, 1e-12 if prec == tcym.FP64 else 1e-6, 400)
+    ref, total = [], 0.0
+    for _ in range(n // stride):
+        P.leapfrog(shape, U, E, dt, stride)
+        total += dt * stride * P.edotb_clover(shape, U, E) / (8 * np.pi ** 2)
+        ref.append(total)
+    ref = np.array(ref)
+    scale = max(np.abs(ref).max(), 1e-3)
+    err = np.abs(series[:, 1] - ref).max() / scale
+    print(f"\nmeasured served request SU(3) 6^3 prec={prec} vs oracle: N_CS {err:.2e} of {scale:.3e}")
+    assert rc == 0 and np.allclose(series[:, 0], [stride * (k + 1) for k in range(n // stride)])
+    assert err < (1e-9 if prec == tcym.FP64 else 1e-5)
 
 
 def test_admission_by_memory_budget(ctx):
