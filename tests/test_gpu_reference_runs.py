@@ -201,7 +201,11 @@ def test_su2_96_cooling_against_reference_run(ctx):
         if name.startswith("FP64"):
             assert mag.max() < 1e-6 and ncs.max() < 1e-6, name
         else:
+            # FP32 storage: the links are renormalised after every sweep; what stays is
+            # an absolute offset of the magnetic energy at the level of the links' norms
+            # (~1e-8), relative to an energy that falls 280-fold over the 500 sweeps
             assert mag[:3].max() < 1e-5 and ncs[:3].max() < 1e-5, name
+            assert mag.max() < 1e-3 and ncs.max() < 1e-4, name
 
 
 def test_energy_drift_fp32_vs_fp64(ctx):

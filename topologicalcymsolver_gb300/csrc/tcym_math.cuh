@@ -40,9 +40,15 @@ namespace tcym {
 template <class T> struct Real;
 template <> struct Real<float> {
     static TCYM_HD float sqrt_(float x) { return sqrtf(x); }
+    // 1/sqrt(x) to about half an ulp: the hardware approximation refined by one
+    // Newton step.  It renormalises FP32 links after every sweep of a gradient
+    // flow, where the approximation's own error (up to 2 ulp, not of either sign
+    // on average) would set every link's norm off 1 the same way and shift a
+    // cooled field's small magnetic energy by a constant.
     static TCYM_HD float rsqrt_(float x) {
 #ifdef __CUDA_ARCH__
-        return rsqrtf(x);
+        const float r = rsqrtf(x);
+        return fmaf(r, fmaf(-0.5f * x * r, r, 0.5f), r);
 #else
         return 1.0f / sqrtf(x);
 #endif
