@@ -31,6 +31,7 @@ def load():
                               ctypes.c_int]
         L.hc_flow_cb.argtypes = [ctypes.c_int, ip, _vp, ctypes.c_double, ctypes.c_int]
         L.hc_observables.argtypes = [ctypes.c_int, ip, _vp, _vp, ctypes.c_int, _vp]
+        L.hc_edotb_pair.argtypes = [ctypes.c_int, ip, _vp, _vp, _vp]
         L.hc_gauss_restore.argtypes = [ctypes.c_int, ip, _vp, _vp, ctypes.c_double, ctypes.c_int]
         L.hc_reunitarize.argtypes = [ctypes.c_int, ip, _vp]
         L.hc_block.argtypes = [ctypes.c_int, ip, _vp, _vp]
@@ -108,6 +109,12 @@ class HostLattice:
         out = np.zeros(16)
         self.L.hc_observables(self.fmt, self.n, _p(self.U[self.cur]), _p(self.E), mask, _p(out))
         return out
+
+    def edotb_pair(self):
+        """The N_CS sample through the paired code, or None where the storage is not paired."""
+        out = np.zeros(16)
+        ok = self.L.hc_edotb_pair(self.fmt, self.n, _p(self.U[self.cur]), _p(self.E), _p(out))
+        return out if ok else None
 
     def gauss_restore(self, tol=1e-14, maxit=10000):
         return self.L.hc_gauss_restore(self.fmt, self.n, _p(self.U[self.cur]), _p(self.E), tol, maxit)

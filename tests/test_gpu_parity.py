@@ -280,6 +280,33 @@ def test_ncs_tracking_is_kahan_sum_of_edotb(ctx, oracle_port, nc):
     assert abs(lat.ncs() - total) < 1e-11 * max(1.0, abs(total))
 
 
+@pytest.mark.parametrize("shape", [(6, 6, 6), (4, 6, 5)], ids=["paired", "odd_nz"])
+@pytest.mark.parametrize("nc", GROUPS)
+def test_ncs_tracking_fp32_against_oracle(ctx, oracle_port, nc, shape):
+    """FP32 storage, N_CS sampled every 2 steps (the paired E.B kernel for even nz, the
+    per-site one for odd nz) against the oracle's Kahan-free sum of dt * 2 * clover
+    E.B / 8 pi^2 over the same 20 steps from the same (FP32-rounded) state: within
+    1e-5 of the sum's scale, 20 dt V |E| |B| / 8 pi^2."""
+    P = oracle_port[nc]
+    U, E = random_state(P, nc, shape, seed=63, sigma_u=0.3)
+    lat = tcym.Lattice(ctx, nc, shape, tcym.FP32)
+    lat.set_reunitarize_period(0)
+    lat.upload(U, E)
+    U, E = lat.download()
+    lat.ncs_track(2)
+    lat.ncs_reset()
+    dt, total = 0.05, 0.0
+    for _ in range(10):
+        lat.leapfrog(dt, 2)
+        P.leapfrog(shape, U, E, dt, 2)
+        total += 2 * dt * P.edotb_clover(shape, U, E) / (8 * np.pi ** 2)
+    o = P.observables(shape, U, E)
+    scale = 20 * dt * np.prod(shape) * 2.0 * np.sqrt(o[1] * o[2]) / (8 * np.pi ** 2)
+    err = abs(lat.ncs() - total) / scale
+    print(f"\nmeasured FP32 N_CS tracking SU({nc}) {shape}: {err:.2e} of {scale:.3e}")
+    assert err < 1e-5
+
+
 def test_error_codes(ctx):
     with pytest.raises(tcym.TcymError) as ei:
         tcym.Lattice(ctx, 4, (4, 4, 4))

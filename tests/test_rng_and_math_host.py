@@ -140,6 +140,29 @@ def test_site_observables_and_restore(oracle_port, nc, prec):
         assert rel(H.download()[1], E) < 1e-12
 
 
+@pytest.mark.parametrize("shape", [(4, 5, 6), (6, 4, 8), (5, 6, 2)])
+@pytest.mark.parametrize("nc", [2, 3])
+def test_paired_edotb_sample(oracle_port, nc, shape):
+    """The N_CS sample of FP32 pair storage through the paired code (both sites of a
+    pair in packed FP32, the z seam's lane swaps) against the per-site code and the
+    oracle on the same (FP32-rounded) state: E^2 and B^2 within 1e-7, clover E.B (a sum
+    that cancels) within 1e-7 of V |E| |B|, the scale of the sum of |E.B| over the
+    sites (measured: 1e-9 and 5e-10 at most)."""
+    P = oracle_port[nc]
+    U, E = _state(P, nc, shape, 19)
+    H = hc.HostLattice(nc, "f32", shape)
+    H.upload(U, E)
+    Ur, Er = H.download()
+    got, per_site, ref = H.edotb_pair(), H.observables(mask=8), P.observables(shape, Ur, Er)
+    assert got is not None
+    scale = np.prod(shape) * 2.0 * np.sqrt(ref[1] * ref[2])  # V |E| |B|
+    for k in (1, 2, 3, 4, 5, 6, 7, 8):
+        assert abs(got[k] - ref[k]) < 1e-7 * max(1.0, abs(ref[k])), (k, got[k], ref[k])
+        assert abs(got[k] - per_site[k]) < 1e-7 * max(1.0, abs(per_site[k])), (k, got[k], per_site[k])
+    assert abs(got[13] - ref[13]) < 1e-7 * max(scale, abs(ref[13])), (got[13], ref[13], scale)
+    assert abs(got[13] - per_site[13]) < 1e-7 * max(scale, abs(per_site[13]))
+
+
 @pytest.mark.parametrize("nc,prec", FORMATS)
 def test_site_improved_edotb(oracle_port, nc, prec):
     P = oracle_port[nc]

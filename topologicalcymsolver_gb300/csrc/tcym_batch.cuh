@@ -255,6 +255,65 @@ __global__ void __launch_bounds__(kThreadsPair, batch_min_blocks_for<FMT>())
 }
 
 // Observables of every member: one partial record per reduction work item.
+// The N_CS sample (mask OBS_EDOTB) of every member: members in FP32 pair storage
+// (even nz) one thread per site pair, the others per site as k_observables_batch.
+// A member keeps its grid_for(V, kRedThreads) records (the finaliser's layout);
+// paired, its first grid_for(V/2, kRedThreads) hold the pairs and the rest zeros.
+template <int FMT>
+__global__ void __launch_bounds__(kRedThreads)
+    k_edotb_obs_batch(const Member<typename Fmt<FMT>::T> *members, int nmembers, int total_blocks, double *partial) {
+    using F = Fmt<FMT>;
+    for (int item = blockIdx.x; item < total_blocks; item += gridDim.x) {
+        const int mi = find_member(members, nmembers, item, true);
+        const Geom g = members[mi].g;
+        const void *u = members[mi].U[members[mi].cur], *e = members[mi].E;
+        double v[P_WIDTH];
+#pragma unroll
+        for (int q = 0; q < P_WIDTH; ++q) v[q] = 0.0;
+        const int64_t i = (int64_t)(item - members[mi].red_begin) * blockDim.x + threadIdx.x;
+        if constexpr (F::PAIRED) {
+            if (members[mi].paired) {
+                const int64_t Vh = g.V >> 1, plane = (int64_t)g.nx * g.ny;
+                if (i < Vh) {
+                    const bool seam = i < plane || i >= Vh - plane;
+#pragma unroll 1
+                    for (int mu = 0; mu < 3; ++mu) {
+                        f2 esq, bsq;
+                        const f2 edb = seam ? pair_edotb_obs<F, true>(g, u, e, i, mu, esq, bsq)
+                                            : pair_edotb_obs<F, false>(g, u, e, i, mu, esq, bsq);
+                        const double es = (double)esq.v.x + (double)esq.v.y, bs = (double)bsq.v.x + (double)bsq.v.y;
+                        if (mu == 0) { v[P_ESQ0] += es; v[P_BSQ0] += bs; }
+                        else if (mu == 1) { v[P_ESQ0 + 1] += es; v[P_BSQ0 + 1] += bs; }
+                        else { v[P_ESQ0 + 2] += es; v[P_BSQ0 + 2] += bs; }
+                        v[P_EDB] += (double)edb.v.x + (double)edb.v.y;
+                    }
+                }
+            }
+        }
+        if (!(F::PAIRED && members[mi].paired) && i < g.V) {
+            SiteObs<F> o;
+            site_observables<F>(g, u, e, OBS_EDOTB, i, o);
+            for (int q = 0; q < 3; ++q) { v[P_ESQ0 + q] = o.esq[q]; v[P_BSQ0 + q] = o.bsq[q]; }
+            v[P_EDB] = o.edotb;
+        }
+        __shared__ double sh[32][P_WIDTH];
+        const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+        for (int q = 0; q < P_WIDTH; ++q) v[q] = q < P_GMAX ? warp_sum(v[q]) : warp_max(v[q]);
+        if (lane == 0)
+#pragma unroll
+            for (int q = 0; q < P_WIDTH; ++q) sh[w][q] = v[q];
+        __syncthreads();
+        if (threadIdx.x < P_WIDTH) {
+            const int q = threadIdx.x;
+            double r = sh[0][q];
+            for (int k = 1; k < nw; ++k) r = q < P_GMAX ? r + sh[k][q] : fmax(r, sh[k][q]);
+            partial[(int64_t)item * P_WIDTH + q] = r;
+        }
+        __syncthreads();
+    }
+}
+
 template <int FMT>
 __global__ void __launch_bounds__(kRedThreads)
     k_observables_batch(const Member<typename Fmt<FMT>::T> *members, int nmembers, int total_blocks, int mask,
@@ -344,6 +403,12 @@ template <int FMT> struct LaunchBatch {
     }
     static cudaError_t observables(const Member<T> *members, int n, int total_blocks, int mask, double *partial,
                                    int grid, cudaStream_t st) {
+        if constexpr (Fmt<FMT>::PAIRED) {
+            if (mask == OBS_EDOTB) {  // the N_CS sample: paired members in packed FP32
+                k_edotb_obs_batch<FMT><<<grid, kRedThreads, 0, st>>>(members, n, total_blocks, partial);
+                return cudaGetLastError();
+            }
+        }
         k_observables_batch<FMT><<<grid, kRedThreads, 0, st>>>(members, n, total_blocks, mask, partial);
         return cudaGetLastError();
     }

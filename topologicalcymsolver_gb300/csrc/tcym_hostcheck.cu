@@ -132,6 +132,33 @@ template <int FMT> struct H {
         out[14] = 0;
         out[15] = gabs;
     }
+    // the N_CS sample through the paired code (FP32 pair storage, even nz): the
+    // E^2, plaquette B^2 and clover E.B slots of observables(); false if not paired
+    static bool edotb_pair(const Geom &g, const void *U, const void *E, double *out) {
+        if constexpr (F::PAIRED) {
+            if (g.nz % 2) return false;
+            double esq[3] = {0, 0, 0}, bsq[3] = {0, 0, 0}, edb = 0;
+            const int64_t Vh = g.V >> 1, plane = (int64_t)g.nx * g.ny;
+            for (int64_t p = 0; p < Vh; ++p)
+                for (int mu = 0; mu < 3; ++mu) {
+                    f2 e2, b2;
+                    const f2 d = (p < plane || p >= Vh - plane) ? pair_edotb_obs<F, true>(g, U, E, p, mu, e2, b2)
+                                                                : pair_edotb_obs<F, false>(g, U, E, p, mu, e2, b2);
+                    esq[mu] += (double)e2.v.x + (double)e2.v.y;
+                    bsq[mu] += (double)b2.v.x + (double)b2.v.y;
+                    edb += (double)d.v.x + (double)d.v.y;
+                }
+            const double V = (double)g.V;
+            for (int k = 0; k < 16; ++k) out[k] = 0;
+            for (int m = 0; m < 3; ++m) { out[3 + m] = esq[m] / V; out[6 + m] = bsq[m] / V; }
+            out[1] = 0.5 * (out[3] + out[4] + out[5]);
+            out[2] = 0.5 * (out[6] + out[7] + out[8]);
+            out[0] = out[1] + out[2];
+            out[13] = edb;
+            return true;
+        }
+        return false;
+    }
     static void iexp_aos(double c, const double *alpha, double *out) {
         T e[F::NA];
         for (int a = 0; a < F::NA; ++a) e[a] = (T)alpha[a];
@@ -244,6 +271,12 @@ int hc_observables(int fmt, const int *n, const void *U, const void *E, int mask
     Geom g = geom(n);
     HC_DISPATCH(fmt, HH::observables(g, U, E, mask, out));
     return 0;
+}
+int hc_edotb_pair(int fmt, const int *n, const void *U, const void *E, double *out) {
+    Geom g = geom(n);
+    int ok = 0;
+    HC_DISPATCH(fmt, ok = HH::edotb_pair(g, U, E, out));
+    return ok;
 }
 int hc_gauss_restore(int fmt, const int *n, const void *U, void *E, double tol, int maxit) {
     Geom g = geom(n);

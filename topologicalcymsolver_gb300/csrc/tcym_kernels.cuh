@@ -240,6 +240,35 @@ __global__ void __launch_bounds__(kRedThreads) k_observables(Geom g, const void 
     block_partial(v, partial);
 }
 
+// The N_CS sample (mask OBS_EDOTB) of FP32 pair storage with even nz: one thread
+// per site pair, the same block partials as k_observables with that mask (the
+// Gauss and unitarity slots stay 0).
+template <int FMT>
+__global__ void __launch_bounds__(kRedThreads) k_edotb_obs_pair(Geom g, const void *U, const void *E,
+                                                                double *partial) {
+    using F = Fmt<FMT>;
+    double v[P_WIDTH];
+#pragma unroll
+    for (int k = 0; k < P_WIDTH; ++k) v[k] = 0.0;
+    const int64_t Vh = g.V >> 1, plane = (int64_t)g.nx * g.ny;
+    for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < Vh; p += (int64_t)gridDim.x * blockDim.x) {
+        const bool seam = p < plane || p >= Vh - plane;
+#pragma unroll 1
+        for (int mu = 0; mu < 3; ++mu) {
+            f2 esq, bsq;
+            const f2 edb = seam ? pair_edotb_obs<F, true>(g, U, E, p, mu, esq, bsq)
+                                : pair_edotb_obs<F, false>(g, U, E, p, mu, esq, bsq);
+            const double es = (double)esq.v.x + (double)esq.v.y, bs = (double)bsq.v.x + (double)bsq.v.y;
+            // fixed slots (a run-time index would put v in local memory)
+            if (mu == 0) { v[P_ESQ0] += es; v[P_BSQ0] += bs; }
+            else if (mu == 1) { v[P_ESQ0 + 1] += es; v[P_BSQ0 + 1] += bs; }
+            else { v[P_ESQ0 + 2] += es; v[P_BSQ0 + 2] += bs; }
+            v[P_EDB] += (double)edb.v.x + (double)edb.v.y;
+        }
+    }
+    block_partial(v, partial);
+}
+
 // Gauss violation into the FP64 scratch G[a*V + s]; partial maxima as for observables.
 template <int FMT>
 __device__ __forceinline__ void gauss_compute_block(const Geom &g, const void *U, const void *E, double *G,
@@ -298,7 +327,6 @@ __global__ void __launch_bounds__(threads_for<FMT>()) k_gauss_update_it(Geom g, 
 // storage's precision; the scratch holds na * V doubles, twice what they need).
 // The per-site sums run in FP32 per thread and the block partials in FP64,
 // with the same signed maximum (fmax drops NaN; the sums keep it).
-TCYM_HD f2 swap_f2(f2 v) { return f2(v.v.y, v.v.x); }
 // 0: the FP32 formats restore through the per-site kernels too
 #ifndef TCYM_RESTORE_PAIRED
 #define TCYM_RESTORE_PAIRED 1
@@ -524,6 +552,12 @@ template <int FMT> struct Launch {
     }
     static cudaError_t observables(const Geom &g, const void *U, const void *E, int mask, double *partial, int blocks,
                                    cudaStream_t st) {
+        if constexpr (Fmt<FMT>::PAIRED) {
+            if (mask == OBS_EDOTB && g.nz % 2 == 0) {  // the N_CS sample: paired FP32
+                k_edotb_obs_pair<FMT><<<blocks, kRedThreads, 0, st>>>(g, U, E, partial);
+                return cudaGetLastError();
+            }
+        }
         k_observables<FMT><<<blocks, kRedThreads, 0, st>>>(g, U, E, mask, partial);
         return cudaGetLastError();
     }

@@ -106,6 +106,8 @@ struct f2 {
     TCYM_HD f2(float a, float b) : v(make_float2(a, b)) {}
 };
 TCYM_HD f2 f2_of(float2 x) { f2 r; r.v = x; return r; }
+// the lanes exchanged (a pair read across the z seam holds its partner's site first)
+TCYM_HD f2 swap_f2(f2 v) { return f2(v.v.y, v.v.x); }
 TCYM_HD f2 operator-(f2 a) { return f2(-a.v.x, -a.v.y); }
 #if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 1000
 #define TCYM_PACKED_FP32 1
