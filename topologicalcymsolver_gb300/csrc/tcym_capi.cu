@@ -883,6 +883,14 @@ extern "C" int tcym_update_u(tcym_lattice lat, double dt) {
     return TCYM_OK;
 }
 
+// 1: FP32 lattices renormalise their links after every flow sweep.  Off: the
+// renormalisation's own rounding sets link norms off 1 by ~1e-8 all one way, which
+// a cooled field's magnetic energy (12 (1 - Re tr U_p / 2) a site) turns into a
+// constant offset near 1e-6; the flow's exponential keeps the links on the group
+// to rounding without it (SU2::iexp_mul, the increment form).
+#ifndef TCYM_FLOW_RENORMALIZE
+#define TCYM_FLOW_RENORMALIZE 0
+#endif
 extern "C" int tcym_flow(tcym_lattice lat, double dtau, int nsteps, int mode, int calibrate, double *dncs) {
     TCYM_RANGE("tcym_flow");
     if (!lat || nsteps < 0 || (mode != TCYM_FLOW_SIMULTANEOUS && mode != TCYM_FLOW_CHECKERBOARD) || calibrate < 0 ||
@@ -923,10 +931,11 @@ extern "C" int tcym_flow(tcym_lattice lat, double dtau, int nsteps, int mode, in
                 for (int mu = 0; mu < 3; ++mu)
                     DISPATCH(lat->fmt, CK(L::flow_cb(lat->g, lat->U[lat->cur], p, mu, c.fc, c.cnu, c.uc, lat->stream)));
         }
-        // FP32 storage: every sweep ends on the group (FP32 renormalisation), so that
-        // rounding does not accumulate into the links over a long flow
+#if TCYM_FLOW_RENORMALIZE
+        // FP32 storage: every sweep ends with its links renormalised in FP32
         if (lat->precision == TCYM_FP32)
             DISPATCH(lat->fmt, CK(L::renormalize(lat->g, lat->U[lat->cur], lat->stream)));
+#endif
         if (calibrate) {
             if ((r = tcym_reduce(lat, op, 0.0))) return r;
             if ((r = fetch_result(lat))) return r;

@@ -432,9 +432,8 @@ template <int FMT> __global__ void k_reunitarize(Geom g, void *U) {
 }
 // FP32 storage: the links of both sites of pair p (s and s + Vh share their
 // vectors) brought back to the group in FP32 arithmetic, rows renormalised
-// (SU(3): Gram-Schmidt, third row rebuilt).  Without it the links of a long FP32
-// gradient flow drift off the group by rounding, and a cooled field's small
-// magnetic energy (1 - Re tr U_p / N per plaquette) follows the drift.
+// (SU(3): Gram-Schmidt, third row rebuilt); run after every gradient-flow sweep
+// when the library is built with TCYM_FLOW_RENORMALIZE=1.
 template <int FMT> __global__ void k_renormalize_pair(Geom g, void *U) {
     using F = Fmt<FMT>;
     const int64_t Vh = pair_sites(g.V);

@@ -163,6 +163,9 @@ TCYM_HD void half_angle(f2 d2, f2 &f, f2 &co) {  // no packed sine: lane by lane
     half_angle(d2.v.x, f.v.x, co.v.x);
     half_angle(d2.v.y, f.v.y, co.v.y);
 }
+TCYM_HD float quot(float a, float b) { return a / b; }
+TCYM_HD double quot(double a, double b) { return a / b; }
+TCYM_HD f2 quot(f2 a, f2 b) { return f2(a.v.x / b.v.x, a.v.y / b.v.y); }
 
 template <class T> struct cx {
     T re, im;
@@ -219,7 +222,21 @@ template <class T> struct SU2 {
     static TCYM_HD Mat mul(const Mat &a, const Mat &b) { return mulx<false, false>(a, b); }
     // product of group elements (same as mulx for SU(2))
     template <bool DA, bool DB> static TCYM_HD Mat mulu(const Mat &a, const Mat &b) { return mulx<DA, DB>(a, b); }
-    static TCYM_HD Mat iexp_mul(T c, const T *e, const Mat &u) { return mul(iexp(c, e), u); }
+    // exp(i c t^k e^k) u formed as u + (exp - 1) u, the real part of exp - 1 being
+    // cos(d/2) - 1 = -sin^2(d/2) / (1 + cos(d/2)), without cancellation.  Near the
+    // identity cos(d/2) rounds to 1 (or next to it) in FP32, which would put |exp|
+    // above 1 by up to sin^2(d/2) at every update, always the same way, and a long
+    // FP32 gradient flow would carry its links off the group; the increment form
+    // leaves only the rounding of u's own components, of either sign.
+    static TCYM_HD Mat iexp_mul(T c, const T *e, const Mat &u) {
+        const T x0 = c * e[0], x1 = c * e[1], x2 = c * e[2];
+        const T d2 = fma(x0, x0, fma(x1, x1, x2 * x2));
+        T f, co;
+        half_angle(d2, f, co);
+        const T cm1 = -quot(f * f * d2, T(1) + co);
+        const Mat w = mul(Mat{{f * x0, f * x1, f * x2, cm1}}, u);
+        return Mat{{u.q[0] + w.q[0], u.q[1] + w.q[1], u.q[2] + w.q[2], u.q[3] + w.q[3]}};
+    }
     // proj(u * a) for the force: Re tr(i t^k (u a)) = -(u a)_k
     static TCYM_HD void proj_mul(const Mat &u, const Mat &a, T *out) {
         Mat w = mulx<false, false>(u, a);
@@ -512,9 +529,12 @@ template <class T> struct SU3 {
     static TCYM_HD Mat iexp(T c, const T *e) { return iexp_hermitian(algebra_matrix(c, e)); }
 
     // exp(i c t^a e^a) u for a link update.  In the common case (spectral radius
-    // of Q <= 1/2, no scaling) only rows 0 and 1 of exp(iQ) and of the product
-    // are formed; row 2 of the product is conj(row0 x row1).  Otherwise the
-    // scaled-and-squared exponential is used.
+    // of Q <= 1/2, no scaling) only rows 0 and 1 of exp(iQ) - 1 and of
+    // u + (exp(iQ) - 1) u are formed; row 2 of the product is conj(row0 x row1).
+    // The increment form keeps f0 - 1 apart from the 1: near the identity f0
+    // itself rounds next to 1 in FP32, which would move every updated link's
+    // norm the same way and carry a long FP32 gradient flow off the group.
+    // Otherwise the scaled-and-squared exponential is used.
     static TCYM_HD Mat iexp_mul(T c, const T *e, const Mat &u) {
         const Mat q = algebra_matrix(c, e);
         // c1 = tr(Q^2)/2 = sum_ij |Q_ij|^2 / 2
@@ -548,12 +568,12 @@ template <class T> struct SU3 {
             // terms of the series by the spectral radius r (r^2 <= 4 c1 / 3): the first
             // omitted term r^(N+1)/(N+1)! stays below half an FP32 ulp, 3e-8, with 5
             // terms for r^2 <= 0.02 (the common case: |dt E| is small) and 8 up to r = 1/2
-            if (any_gt(c1 * T(4.0 / 3.0), T(0.02))) series_coeffs<8>(c0, c1, f0r, f0i, f1r, f1i, f2r, f2i);
-            else series_coeffs<5>(c0, c1, f0r, f0i, f1r, f1i, f2r, f2i);
+            if (any_gt(c1 * T(4.0 / 3.0), T(0.02))) series_coeffs<8, true>(c0, c1, f0r, f0i, f1r, f1i, f2r, f2i);
+            else series_coeffs<5, true>(c0, c1, f0r, f0i, f1r, f1i, f2r, f2i);
         } else {
-            series_coeffs<16>(c0, c1, f0r, f0i, f1r, f1i, f2r, f2i);
+            series_coeffs<16, true>(c0, c1, f0r, f0i, f1r, f1i, f2r, f2i);
         }
-        Mat w;
+        Mat w;  // rows 0 and 1 of exp(iQ) - 1
 #pragma unroll
         for (int i = 0; i < 2; ++i)
 #pragma unroll
@@ -564,7 +584,22 @@ template <class T> struct SU3 {
                 if (i == j) { re += f0r; im += f0i; }
                 w.m[i][j] = cx<T>{re, im};
             }
-        return mulu<false, false>(w, u);  // reads rows 0 and 1 of w only
+        return mulu_inc(w, u);  // reads rows 0 and 1 of w only
+    }
+    // rows 0 and 1 of u + w u (each accumulator starts at u's entry), row 2 rebuilt
+    static TCYM_HD Mat mulu_inc(const Mat &w, const Mat &u) {
+        Mat r;
+#pragma unroll
+        for (int i = 0; i < 2; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                cx<T> acc = u.m[i][j];
+#pragma unroll
+                for (int k = 0; k < 3; ++k) acc = cfma(w.m[i][k], u.m[k][j], acc);
+                r.m[i][j] = acc;
+            }
+        complete_row2(r);
+        return r;
     }
     // packed pairs whose exponent needs scaling: each lane through the scalar path
     template <class P = T> static TCYM_COLD Mat iexp_mul_lanes(P c, const P *e, const Mat &u) {
@@ -593,14 +628,16 @@ template <class T> struct SU3 {
 
     // f_k of exp(iQ) = f0 + f1 Q + f2 Q^2 for spectral radius <= 1/2: the Taylor
     // series reduced with Q^3 = c1 Q + c0 (Q^n = a_n + b_n Q + d_n Q^2).
-    template <int N> static TCYM_HD void series_coeffs(T c0, T c1, T &f0r, T &f0i, T &f1r, T &f1i, T &f2r, T &f2i) {
+    // M1: f0r returns f0 - 1 (the series without its leading 1), for the increment form
+    template <int N, bool M1 = false>
+    static TCYM_HD void series_coeffs(T c0, T c1, T &f0r, T &f0i, T &f1r, T &f1i, T &f2r, T &f2i) {
         static_assert(N >= 1 && N <= 16, "at most 16 terms");
         constexpr double inv_fact[17] = {1.0, 1.0, 0.5, 1.0 / 6, 1.0 / 24, 1.0 / 120, 1.0 / 720, 1.0 / 5040,
                                          1.0 / 40320, 1.0 / 362880, 1.0 / 3628800, 1.0 / 39916800,
                                          1.0 / 479001600, 1.0 / 6227020800.0, 1.0 / 87178291200.0,
                                          1.0 / 1307674368000.0, 1.0 / 20922789888000.0};
         T a = T(1), b = T(0), d = T(0);
-        f0r = T(1); f0i = T(0); f1r = T(0); f1i = T(0); f2r = T(0); f2i = T(0);
+        f0r = M1 ? T(0) : T(1); f0i = T(0); f1r = T(0); f1i = T(0); f2r = T(0); f2i = T(0);
 #pragma unroll
         for (int n = 1; n <= N; ++n) {
             const T na = d * c0, nb = fma(d, c1, a), nd = b;
