@@ -201,11 +201,12 @@ def test_su2_96_cooling_against_reference_run(ctx):
         if name.startswith("FP64"):
             assert mag.max() < 1e-6 and ncs.max() < 1e-6, name
         else:
-            # FP32 storage holds the links' norms to rounding, ~1e-8 an update; the cooled
-            # field's magnetic energy (12 (1 - Re tr U_p / 2) a site) falls 280-fold over
-            # the 500 sweeps to 4e-4 a site, where that rounding is ~1e-3 of it
+            # FP32 storage: the cooled field's magnetic energy (12 (1 - Re tr U_p / 2) a
+            # site) falls 280-fold over the 500 sweeps to 4e-4 a site, and follows the
+            # links' norms to first order; the exponentials' increment form keeps those
+            # unbiased (measured: magnetic 4e-7 over 30 sweeps, 6.7e-5 over 500; N_CS 4e-6)
             assert mag[:3].max() < 1e-5 and ncs[:3].max() < 1e-5, name
-            assert mag.max() < 1e-2 and ncs.max() < 1e-4, name
+            assert mag.max() < 1e-3 and ncs.max() < 5e-5, name
 
 
 def test_energy_drift_fp32_vs_fp64(ctx):
