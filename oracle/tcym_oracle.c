@@ -6,7 +6,7 @@
  * restore, observables, clover E.B), in plain C with OpenMP over z as the
  * reference parallelises (DYNAMICS/Dynamics.cpp:106-136).  Only tests/,
  * __graft_entry__.smoke() and bench.py's CPU-baseline / reference arm load it,
- * as the checker.  The CUDA product never links or calls it.
+ * to check or time against.  The CUDA product never links or calls it.
  *
  * Parity pin: this restatement is checked in tests/test_oracle_golden.py
  * against golden vectors produced by the reference's own sources compiled
