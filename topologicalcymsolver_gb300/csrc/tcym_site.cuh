@@ -526,9 +526,10 @@ TCYM_HD void site_observables(const Geom &g, const void *U, const void *E, int m
 // pair p of FP32 pair storage (even nz), in packed FP32 (lane 0: site p, lane 1:
 // its partner p + Vh): E_mu^2 into esq, the plaquette term of B_mu^2 into bsq, and
 // the clover E_mu . B_mu returned, as site_observables forms them.  SEAM: the pair
-// may step across the z seam, where a neighbour's lanes come swapped.  Each clover
-// leaf is a left-to-right chain of products (one link loaded at a time), the leaves
-// summed one by one, E.B accumulated in FP32 per site.
+// may step across the z seam, where a neighbour's lanes come swapped.  The clover
+// average's projection is the average of the leaves' projections (proj is linear),
+// so each leaf is a left-to-right chain of products whose last one is projected
+// at once (proj_mul, proj_mul_dag) and no 3x3 sum is held; E.B accumulates in FP32.
 template <class F, bool SEAM>
 TCYM_HD f2 pair_edotb_obs(const Geom &g, const void *U, const void *E, int64_t p, int mu, f2 &esq, f2 &bsq) {
     using G2 = typename F::G2;
@@ -541,25 +542,39 @@ TCYM_HD f2 pair_edotb_obs(const Geom &g, const void *U, const void *E, int64_t p
     auto L = [&](int d, int a, int b) {
         return F::load2(U, Vh, d, nb.at(j, a, k, b), SEAM && nb.swapped(j, a, k, b));
     };
-    // Q0 = U_j(x) U_k(x+j) U_j^dag(x+k) U_k^dag(x)
-    M2 t = G2::mul(L(j, 0, 0), L(k, 1, 0));
-    t = G2::template mulx<false, true>(t, L(j, 0, 1));
-    M2 acc = G2::template mulx<false, true>(t, L(k, 0, 0));
-    bsq = f2(4.0) * G2::retr_one_minus(acc);
-    // Q1 = U_k(x) U_j^dag(x+k-j) U_k^dag(x-j) U_j(x-j)
-    t = G2::template mulx<false, true>(L(k, 0, 0), L(j, -1, 1));
-    t = G2::template mulx<false, true>(t, L(k, -1, 0));
-    acc = G2::add(acc, G2::mul(t, L(j, -1, 0)));
-    // Q2 = U_k^dag(x-k) U_j(x-k) U_k(x-k+j) U_j^dag(x)
-    t = G2::template mulx<true, false>(L(k, 0, -1), L(j, 0, -1));
-    t = G2::mul(t, L(k, 1, -1));
-    acc = G2::add(acc, G2::template mulx<false, true>(t, L(j, 0, 0)));
-    // Q3 = U_j^dag(x-j) U_k^dag(x-j-k) U_j(x-j-k) U_k(x-k)
-    t = G2::template mulx<true, true>(L(j, -1, 0), L(k, -1, -1));
-    t = G2::mul(t, L(j, -1, -1));
-    acc = G2::add(acc, G2::mul(t, L(k, 0, -1)));
-    f2 b[NA];
-    G2::proj(G2::scale(f2(0.25), acc), b);
+    f2 b[NA], pr[NA];
+    {
+        // Q0 = U_j(x) U_k(x+j) U_j^dag(x+k) U_k^dag(x), whole: its trace is the plaquette term
+        M2 t = G2::mul(L(j, 0, 0), L(k, 1, 0));
+        t = G2::template mulx<false, true>(t, L(j, 0, 1));
+        const M2 q0 = G2::template mulx<false, true>(t, L(k, 0, 0));
+        bsq = f2(4.0) * G2::retr_one_minus(q0);
+        G2::proj(q0, b);
+    }
+    {
+        // Q1 = U_k(x) U_j^dag(x+k-j) U_k^dag(x-j) U_j(x-j)
+        M2 t = G2::template mulx<false, true>(L(k, 0, 0), L(j, -1, 1));
+        t = G2::template mulx<false, true>(t, L(k, -1, 0));
+        G2::proj_mul(t, L(j, -1, 0), pr);
+#pragma unroll
+        for (int a = 0; a < NA; ++a) b[a] = b[a] + pr[a];
+    }
+    {
+        // Q2 = U_k^dag(x-k) U_j(x-k) U_k(x-k+j) U_j^dag(x)
+        M2 t = G2::template mulx<true, false>(L(k, 0, -1), L(j, 0, -1));
+        t = G2::mul(t, L(k, 1, -1));
+        G2::proj_mul_dag(t, L(j, 0, 0), pr);
+#pragma unroll
+        for (int a = 0; a < NA; ++a) b[a] = b[a] + pr[a];
+    }
+    {
+        // Q3 = U_j^dag(x-j) U_k^dag(x-j-k) U_j(x-j-k) U_k(x-k)
+        M2 t = G2::template mulx<true, true>(L(j, -1, 0), L(k, -1, -1));
+        t = G2::mul(t, L(j, -1, -1));
+        G2::proj_mul(t, L(k, 0, -1), pr);
+#pragma unroll
+        for (int a = 0; a < NA; ++a) b[a] = f2(0.25) * (b[a] + pr[a]);
+    }
     // E_mu(x) and U_mu^dag(x-mu) E_mu(x-mu) U_mu(x-mu)
     f2 e[NA], et[NA];
     {
