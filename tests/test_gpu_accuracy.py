@@ -119,7 +119,7 @@ def test_ncs_diffusion_su3_fp32_vs_fp64_and_oracle(ctx, oracle_port):
     """The SU(3) N_CS diffusion of 256 Langevin trajectories (16^3, 2000 steps at T 0.6):
     <(Delta N_CS)^2> with a standard error of at most 10% of its value (measured 7.9%);
     the FP32-storage ensemble against the FP64 one (the same starts and noise) through
-    the paired difference (measured 6e-5 +- 3e-4 on 5.39), and four FP64 members
+    the paired difference (measured 1.5e-4 +- 3.0e-4 and 4.9e-4 +- 3.8e-4 on 5.39), and four FP64 members
     against the oracle's N_CS series and fields."""
     n, L, steps, every = 256, 16, 2000, 20
     ncs, ends = {}, {}
