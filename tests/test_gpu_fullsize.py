@@ -144,9 +144,9 @@ def test_energy_drift_1e4_steps_at_128_fp32(ctx):
     """The FP32-storage step holds |dE/E| <= 1e-6 over 10^4 steps at 128^3 to the
     resolution the fluctuating energy allows: over four starts, the halves of each run
     differ by a few 1e-6 with either sign (the leapfrog energy's fluctuation at this
-    volume, a half's mean carrying a standard error near 0.9e-6; measured -3.1e-6 ..
-    1.6e-6 over eight starts, and -1.9e-6 .. 1.3e-6 for the previous staple form of the
-    step) and their mean is within 2e-6 of zero."""
+    volume, correlated over many samples: the FP64 run moves by -2.7e-6; measured
+    -2.7e-7 .. 3.9e-6, mean 1.5e-6, and -3.1e-6 .. 1.6e-6 over eight starts before the
+    link updates took the increment form) and their mean is within 2e-6 of zero."""
     runs = [_drift(ctx, tcym.FP32, seed) for seed in range(4)]
     halves = np.array([h for h, _ in runs])
     fits = np.array([f for _, f in runs])
@@ -158,7 +158,7 @@ def test_energy_drift_1e4_steps_at_128_fp32(ctx):
 
 def test_energy_drift_1e4_steps_at_128_fp64(ctx):
     """The plain FP64 step over the same 10^4 steps (one start: 130 s): the same
-    bounds per run (measured halves -1.1e-6, fit -1.0e-6)."""
+    bounds per run (measured halves -2.7e-6, fit -2.3e-6)."""
     halves, fit = _drift(ctx, tcym.FP64, 0)
     print(f"\nmeasured FP64 energy drift over 1e4 steps at 128^3: halves {halves:.2e}, fit {fit:.2e}")
     assert abs(halves) <= 5e-6 and abs(fit) <= 1.2e-5
