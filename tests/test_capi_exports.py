@@ -83,3 +83,33 @@ def test_host_alloc_fails_cleanly_without_gpu():
     assert L.tcym_host_alloc(0, ctypes.byref(p)) == 0 and not p.value
     L.tcym_host_free.argtypes = [ctypes.c_void_p]
     assert L.tcym_host_free(None) == 0
+
+
+def test_python_structures_match_the_header(tmp_path):
+    """The ctypes/numpy mirrors of the header's structures have its sizes and offsets
+    (a C program compiled against include/tcym.h prints them)."""
+    import shutil
+    import subprocess
+
+    import numpy as np
+
+    import topologicalcymsolver_gb300 as tcym
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    src = tmp_path / "layout.c"
+    src.write_text(
+        "#include <stddef.h>\n#include <stdio.h>\n#include \"tcym.h\"\n"
+        "int main(void) { printf(\"%zu %zu %zu %zu %zu %zu\\n\", sizeof(tcym_tick), offsetof(tcym_tick, ms),"
+        " offsetof(tcym_tick, gap_ms), offsetof(tcym_tick, link_updates), offsetof(tcym_tick, active),"
+        " offsetof(tcym_tick, preparing)); return 0; }\n")
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    size, *offs = (int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True,
+                                                   check=True).stdout.split())
+    dt = tcym.TICK_DTYPE
+    assert dt.itemsize == size
+    assert [dt.fields[n][1] for n in ("ms", "gap_ms", "link_updates", "active", "preparing")] == offs
+    assert dt.fields["active"][0] == np.dtype(np.int32)
+
