@@ -430,19 +430,6 @@ template <int FMT> __global__ void k_reunitarize(Geom g, void *U) {
     int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (s < g.V) site_reunitarize<Fmt<FMT>>(g, U, s);
 }
-// FP32 storage: the links of both sites of pair p (s and s + Vh share their
-// vectors) brought back to the group in FP32 arithmetic, rows renormalised
-// (SU(3): Gram-Schmidt, third row rebuilt); run after every gradient-flow sweep
-// when the library is built with TCYM_FLOW_RENORMALIZE=1.
-template <int FMT> __global__ void k_renormalize_pair(Geom g, void *U) {
-    using F = Fmt<FMT>;
-    const int64_t Vh = pair_sites(g.V);
-    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= Vh) return;
-    for (int64_t s = p; s < g.V; s += Vh)
-#pragma unroll 1
-        for (int mu = 0; mu < 3; ++mu) F::store(U, g.V, mu, s, F::G::reunitarize(F::load(U, g.V, mu, s)));
-}
 template <int FMT>
 __global__ void k_geodesic(Geom g, const void *Uold, const void *Unew, double c, void *Umid, void *Emid) {
     int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -622,14 +609,6 @@ template <int FMT> struct Launch {
     static cudaError_t reunitarize(const Geom &g, void *U, cudaStream_t st) {
         k_reunitarize<FMT><<<grid_for(g.V, 128), 128, 0, st>>>(g, U);
         return cudaGetLastError();
-    }
-    // FP32 formats: links renormalised in FP32 (a gradient-flow sweep's epilogue); FP64: nothing
-    static cudaError_t renormalize(const Geom &g, void *U, cudaStream_t st) {
-        if constexpr (Fmt<FMT>::PAIRED) {
-            k_renormalize_pair<FMT><<<grid_for(pair_sites(g.V), 128), 128, 0, st>>>(g, U);
-            return cudaGetLastError();
-        }
-        return cudaSuccess;
     }
     // sites [s0, s0 + n) (n < 0: all)
     static cudaError_t from_aos(const Geom &g, void *U, void *E, const double *Ua, const double *Ea, cudaStream_t st,

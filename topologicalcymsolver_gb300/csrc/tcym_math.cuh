@@ -41,10 +41,7 @@ template <class T> struct Real;
 template <> struct Real<float> {
     static TCYM_HD float sqrt_(float x) { return sqrtf(x); }
     // 1/sqrt(x) to about half an ulp: the hardware approximation refined by one
-    // Newton step.  It renormalises FP32 links after every sweep of a gradient
-    // flow, where the approximation's own error (up to 2 ulp, not of either sign
-    // on average) would set every link's norm off 1 the same way and shift a
-    // cooled field's small magnetic energy by a constant.
+    // Newton step (its own error, up to 2 ulp, need not average to zero).
     static TCYM_HD float rsqrt_(float x) {
 #ifdef __CUDA_ARCH__
         const float r = rsqrtf(x);
