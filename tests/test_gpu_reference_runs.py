@@ -203,10 +203,11 @@ def test_su2_96_cooling_against_reference_run(ctx):
         else:
             # FP32 storage: the cooled field's magnetic energy (12 (1 - Re tr U_p / 2) a
             # site) falls 280-fold over the 500 sweeps to 4e-4 a site, and follows the
-            # links' norms to first order; the exponentials' increment form keeps those
-            # unbiased (measured: magnetic 4e-7 over 30 sweeps, 6.7e-5 over 500; N_CS 4e-6)
-            assert mag[:3].max() < 1e-5 and ncs[:3].max() < 1e-5, name
-            assert mag.max() < 1e-3 and ncs.max() < 5e-5, name
+            # links' norms to first order; the increment-form exponentials and the FP64
+            # reunitarisation every 10 sweeps keep them (measured: magnetic 6.5e-8 over
+            # 30 sweeps, 3.3e-6 over 500; N_CS 2.9e-6)
+            assert mag[:3].max() < 1e-6 and ncs[:3].max() < 1e-5, name
+            assert mag.max() < 5e-5 and ncs.max() < 5e-5, name
 
 
 def test_energy_drift_fp32_vs_fp64(ctx):
