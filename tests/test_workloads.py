@@ -35,3 +35,29 @@ def test_request_stream_distribution():
     h, _ = np.histogram(np.log(steps), bins=5)
     assert h.min() > 0.7 * h.mean()
     assert len({r["seed"] for r in reqs}) == 2000
+
+
+def test_tick_summary_splits_time_and_rates():
+    """The serve workload's summary of the server's tick log: the link-update rate inside
+    ticks, the share of wall time inside them, and both split by whether a preparation
+    was under way, from records laid out as tcym_tick."""
+    import numpy as np
+
+    import topologicalcymsolver_gb300 as tcym
+    from topologicalcymsolver_gb300 import workloads
+
+    log = np.zeros(4, dtype=tcym.TICK_DTYPE)
+    log["ms"] = [100.0, 100.0, 200.0, 100.0]
+    log["gap_ms"] = [0.0, 10.0, 10.0, 80.0]
+    log["link_updates"] = [1e9, 1e9, 1e9, 2e9]
+    log["active"] = [3, 3, 4, 5]
+    log["preparing"] = [0, 1, 1, 0]
+    s = workloads._tick_summary(log)
+    assert s["ticks"] == 4 and abs(s["wall_s"] - 0.6) < 1e-12
+    assert abs(s["share_in_ticks"] - 500.0 / 600.0) < 1e-12
+    assert abs(s["in_tick_link_updates_per_s"] - 5e9 / 0.5) < 1e-3
+    assert abs(s["in_tick_link_updates_per_s_while_preparing"] - 2e9 / 0.3) < 1e-3
+    assert abs(s["in_tick_link_updates_per_s_preparers_idle"] - 3e9 / 0.2) < 1e-3
+    assert s["ticks_while_preparing"] == 2 and s["ticks_preparers_idle"] == 2
+    assert abs(s["gap_ms_total_s"] - 0.1) < 1e-12 and s["active_median"] == 3.5
+    assert workloads._tick_summary(log[:0]) is None
